@@ -1,0 +1,584 @@
+// capi.cpp -- the extern "C" entry points of libfpg.so (declared in include/fpg.h).
+//
+// Host side of the engine: argument checks (same conditions as the
+// reference's std::invalid_argument checks), string encoding and x-grouping,
+// launch planning, stream-ordered scratch memory and kernel dispatch.
+#include "fpg.h"
+
+#include <algorithm>
+#include <initializer_list>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "host_internal.hpp"
+
+using namespace fpg;
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+
+static thread_local std::string g_last_error;
+
+namespace fpg
+{
+int set_error(int code, const std::string &msg)
+{
+    g_last_error = msg;
+    return code;
+}
+int cuda_error(cudaError_t e, const char *where)
+{
+    return set_error(FPG_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+} // namespace fpg
+
+#define FPG_CUDA(call)                                                                                                 \
+    do                                                                                                                 \
+    {                                                                                                                  \
+        cudaError_t e_ = (call);                                                                                       \
+        if (e_ != cudaSuccess)                                                                                         \
+            return cuda_error(e_, #call);                                                                              \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// operator encoding
+// ---------------------------------------------------------------------------
+
+namespace fpg
+{
+
+int encode_strings(const char *strings, int64_t P, int n, std::vector<StringRec> &recs, std::vector<int32_t> &orig,
+                   std::vector<Group> &groups, std::vector<Chunk> &chunks, std::vector<int> &class_begin)
+{
+    std::vector<StringRec> raw((size_t)P);
+    for (int64_t j = 0; j < P; ++j)
+    {
+        uint64_t x = 0, z = 0;
+        uint32_t ny = 0;
+        for (int q = 0; q < n; ++q)
+        {
+            const char c = strings[j * n + q];
+            const uint64_t bit = 1ull << (n - 1 - q);
+            switch (c)
+            {
+            case 'I': break;
+            case 'X': x |= bit; break;
+            case 'Y': x |= bit; z |= bit; ++ny; break;
+            case 'Z': z |= bit; break;
+            default:
+                return set_error(FPG_ERR_INVALID, std::string("Invalid Pauli character ") + c);
+            }
+        }
+        uint32_t ml = 0;
+        for (uint32_t r = 0; r < 32; ++r)
+            ml |= (uint32_t)(__builtin_popcountll((uint64_t)r & z & 31ull) & 1) << r;
+        raw[(size_t)j] = StringRec{x, z, ml, ny & 3u};
+    }
+    std::vector<int32_t> idx((size_t)P);
+    for (int64_t j = 0; j < P; ++j)
+        idx[(size_t)j] = (int32_t)j;
+    std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) {
+        const StringRec &ra = raw[(size_t)a], &rb = raw[(size_t)b];
+        if (ra.x != rb.x)
+            return ra.x < rb.x;
+        const uint32_t pa = ra.meta & 1u, pb = rb.meta & 1u;
+        if (pa != pb)
+            return pa < pb;
+        return ra.z < rb.z;
+    });
+    recs.resize((size_t)P);
+    orig.resize((size_t)P);
+    for (int64_t s = 0; s < P; ++s)
+    {
+        recs[(size_t)s] = raw[(size_t)idx[(size_t)s]];
+        orig[(size_t)s] = idx[(size_t)s];
+    }
+    groups.clear();
+    for (int64_t s = 0; s < P;)
+    {
+        int64_t e = s;
+        while (e < P && recs[(size_t)e].x == recs[(size_t)s].x)
+            ++e;
+        groups.push_back(Group{recs[(size_t)s].x, (int32_t)s, (int32_t)(e - s)});
+        s = e;
+    }
+    // chunks of each group, bucketed by kernel class
+    std::vector<std::vector<Chunk>> by_class(kNumChunkClasses);
+    for (const Group &g : groups)
+    {
+        int32_t ev_b = g.begin, ev_e = g.begin;
+        while (ev_e < g.begin + g.count && (recs[(size_t)ev_e].meta & 1u) == 0)
+            ++ev_e;
+        int32_t od_b = ev_e, od_e = g.begin + g.count;
+        while (ev_b < ev_e || od_b < od_e)
+        {
+            const int ne = std::min<int32_t>(8, ev_e - ev_b);
+            const int no = std::min<int32_t>(8, od_e - od_b);
+            const int cls = chunk_class_for(ne, no);
+            Chunk c{};
+            c.x = g.x;
+            c.begin_even = ev_b;
+            c.begin_odd = od_b;
+            c.n_even = (int16_t)ne;
+            c.n_odd = (int16_t)no;
+            by_class[(size_t)cls].push_back(c);
+            ev_b += ne;
+            od_b += no;
+        }
+    }
+    chunks.clear();
+    class_begin.assign(kNumChunkClasses + 1, 0);
+    for (int c = 0; c < kNumChunkClasses; ++c)
+    {
+        class_begin[(size_t)c] = (int)chunks.size();
+        chunks.insert(chunks.end(), by_class[(size_t)c].begin(), by_class[(size_t)c].end());
+    }
+    class_begin[kNumChunkClasses] = (int)chunks.size();
+    return FPG_OK;
+}
+
+} // namespace fpg
+
+struct fpg_operator
+{
+    int n = 0;
+    int64_t P = 0;
+    int device = 0;
+    std::vector<StringRec> recs;
+    std::vector<int32_t> orig;
+    std::vector<Group> groups;
+    std::vector<Chunk> chunks;
+    std::vector<int> class_begin;
+    StringRec *d_recs = nullptr;
+    int32_t *d_orig = nullptr;
+    Group *d_groups = nullptr;
+    Chunk *d_chunks = nullptr;
+
+    DevOp dev() const
+    {
+        return DevOp{n, P, (int64_t)groups.size(), d_recs, d_orig, d_groups};
+    }
+};
+
+namespace
+{
+
+struct DeviceGuard
+{
+    int prev = -1;
+    bool ok = true;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess)
+        {
+            ok = false;
+            return;
+        }
+        if (prev != dev && cudaSetDevice(dev) != cudaSuccess)
+            ok = false;
+    }
+    ~DeviceGuard()
+    {
+        if (prev >= 0)
+            cudaSetDevice(prev);
+    }
+};
+
+template <typename T> cudaError_t upload(T **dptr, const std::vector<T> &v)
+{
+    *dptr = nullptr;
+    if (v.empty())
+        return cudaSuccess;
+    cudaError_t e = cudaMalloc((void **)dptr, v.size() * sizeof(T));
+    if (e != cudaSuccess)
+        return e;
+    return cudaMemcpy(*dptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+void free_dev(fpg_operator *op)
+{
+    cudaFree(op->d_recs);
+    cudaFree(op->d_orig);
+    cudaFree(op->d_groups);
+    cudaFree(op->d_chunks);
+    op->d_recs = nullptr;
+    op->d_orig = nullptr;
+    op->d_groups = nullptr;
+    op->d_chunks = nullptr;
+}
+
+int check_dtype(int32_t dtype)
+{
+    if (dtype != FPG_C128 && dtype != FPG_C64)
+        return set_error(FPG_ERR_INVALID, "dtype must be FPG_C128 or FPG_C64");
+    return FPG_OK;
+}
+
+// Complex arrays are read with vector loads of one element (16 B complex128,
+// 8 B complex64); a misaligned pointer is an argument error, never a fault.
+int check_aligned(int32_t dtype, std::initializer_list<const void *> ptrs)
+{
+    const uintptr_t a = dtype == FPG_C64 ? 8 : 16;
+    for (const void *p : ptrs)
+        if (p && ((uintptr_t)p % a) != 0)
+            return set_error(FPG_ERR_INVALID, "complex arrays must be aligned to their element size");
+    return FPG_OK;
+}
+
+// Stream-ordered scratch allocation, freed on scope exit (also stream ordered).
+struct Scratch
+{
+    void *p = nullptr;
+    cudaStream_t st;
+    explicit Scratch(cudaStream_t s) : st(s)
+    {
+    }
+    cudaError_t alloc(size_t bytes)
+    {
+        return cudaMallocAsync(&p, bytes ? bytes : 16, st);
+    }
+    ~Scratch()
+    {
+        if (p)
+            cudaFreeAsync(p, st);
+    }
+};
+
+int pick_tc(int64_t lanes)
+{
+    int tc = 1;
+    while (tc < 32 && tc < lanes)
+        tc <<= 1;
+    return tc;
+}
+
+ExpectPlan plan_expect(const fpg_operator *op, int64_t S, bool fp32, const void *psi)
+{
+    ExpectPlan p{};
+    p.V = (fp32 && (S % 2 == 0) && (((uintptr_t)psi) % 16 == 0)) ? 2 : 1;
+    const int64_t lanes = (S + p.V - 1) / p.V;
+    p.TC = pick_tc(lanes);
+    p.n_ctiles = (int)((S + (int64_t)p.TC * p.V - 1) / ((int64_t)p.TC * p.V));
+    const int TR = 256 / p.TC;
+    const int64_t n_chunks = (int64_t)op->chunks.size();
+    const int64_t ctas = n_chunks * p.n_ctiles;
+    const int64_t NB = op->n >= 5 ? ((int64_t)1 << (op->n - 5)) : 1;
+    const int64_t target = 152 * 8; // CTAs in flight: ~8 resident per SM
+    int64_t splits = (target + ctas - 1) / std::max<int64_t>(ctas, 1);
+    const int64_t max_splits = std::max<int64_t>(1, NB / (2 * (int64_t)TR * 4)); // >= 4 blocks per row lane
+    splits = std::max<int64_t>(1, std::min(splits, max_splits));
+    splits = std::min<int64_t>(splits, 65535);
+    p.n_splits = (int)splits;
+    return p;
+}
+
+int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int64_t S, bool fp32, cudaStream_t st)
+{
+    if (S <= 0 || op->P <= 0)
+        return FPG_OK;
+    const ExpectPlan plan = plan_expect(op, S, fp32, psi);
+    const DevOp dop = op->dev();
+    Scratch partial(st);
+    double *dst = ev;
+    if (plan.n_splits > 1)
+    {
+        FPG_CUDA(partial.alloc((size_t)plan.n_splits * (size_t)op->P * (size_t)S * sizeof(double)));
+        dst = (double *)partial.p;
+    }
+    for (int c = 0; c < kNumChunkClasses; ++c)
+    {
+        const int b = op->class_begin[(size_t)c], e = op->class_begin[(size_t)c + 1];
+        if (e > b)
+            FPG_CUDA(launch_expect_chunks(fp32, psi, S, op->n, dop, op->d_chunks + b, e - b, c, plan, dst, st));
+    }
+    if (plan.n_splits > 1)
+        FPG_CUDA(launch_reduce_splits(dst, plan.n_splits, op->P * S, ev, st));
+    return FPG_OK;
+}
+
+} // namespace
+
+// ---------------------------------------------------------------------------
+// entry points
+// ---------------------------------------------------------------------------
+
+extern "C"
+{
+
+    int fpg_abi_version(void)
+    {
+        return FPG_ABI_VERSION;
+    }
+
+    const char *fpg_last_error(void)
+    {
+        return g_last_error.c_str();
+    }
+
+    int fpg_device_count(int *count)
+    {
+        if (!count)
+            return set_error(FPG_ERR_INVALID, "count is null");
+        int c = 0;
+        cudaError_t e = cudaGetDeviceCount(&c);
+        if (e != cudaSuccess)
+        {
+            cudaGetLastError();
+            c = 0;
+        }
+        *count = c;
+        return FPG_OK;
+    }
+
+    int fpg_pointer_is_device(const void *ptr, int *is_device)
+    {
+        if (!is_device)
+            return set_error(FPG_ERR_INVALID, "is_device is null");
+        *is_device = 0;
+        if (!ptr)
+            return FPG_OK;
+        cudaPointerAttributes a{};
+        cudaError_t e = cudaPointerGetAttributes(&a, ptr);
+        if (e != cudaSuccess)
+        {
+            cudaGetLastError();
+            return FPG_OK;
+        }
+        *is_device = (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) ? 1 : 0;
+        return FPG_OK;
+    }
+
+    int fpg_operator_create(const char *strings, int64_t n_strings, int32_t n_qubits, fpg_operator **out)
+    {
+        if (!out)
+            return set_error(FPG_ERR_INVALID, "out is null");
+        *out = nullptr;
+        if (n_strings < 0)
+            return set_error(FPG_ERR_INVALID, "n_strings must be >= 0");
+        if (n_strings > 0 && !strings)
+            return set_error(FPG_ERR_INVALID, "strings is null");
+        if (n_qubits < 1 || n_qubits > 40)
+            return set_error(FPG_ERR_UNSUPPORTED, "n_qubits must be in [1, 40]");
+        if (n_strings > (int64_t)0x7fffffff)
+            return set_error(FPG_ERR_UNSUPPORTED, "too many strings");
+        fpg_operator *op = new (std::nothrow) fpg_operator();
+        if (!op)
+            return set_error(FPG_ERR_NOMEM, "host allocation failed");
+        op->n = n_qubits;
+        op->P = n_strings;
+        int rc = encode_strings(strings, n_strings, n_qubits, op->recs, op->orig, op->groups, op->chunks,
+                                op->class_begin);
+        if (rc != FPG_OK)
+        {
+            delete op;
+            return rc;
+        }
+        cudaError_t e = cudaGetDevice(&op->device);
+        if (e == cudaSuccess)
+            e = upload(&op->d_recs, op->recs);
+        if (e == cudaSuccess)
+            e = upload(&op->d_orig, op->orig);
+        if (e == cudaSuccess)
+            e = upload(&op->d_groups, op->groups);
+        if (e == cudaSuccess)
+            e = upload(&op->d_chunks, op->chunks);
+        if (e != cudaSuccess)
+        {
+            free_dev(op);
+            delete op;
+            return cuda_error(e, "fpg_operator_create");
+        }
+        *out = op;
+        return FPG_OK;
+    }
+
+    int fpg_operator_destroy(fpg_operator *op)
+    {
+        if (!op)
+            return FPG_OK;
+        {
+            DeviceGuard g(op->device);
+            free_dev(op);
+        }
+        delete op;
+        return FPG_OK;
+    }
+
+    int fpg_operator_info(const fpg_operator *op, int32_t *n_qubits, int64_t *n_strings, int64_t *n_groups)
+    {
+        if (!op)
+            return set_error(FPG_ERR_INVALID, "op is null");
+        if (n_qubits)
+            *n_qubits = op->n;
+        if (n_strings)
+            *n_strings = op->P;
+        if (n_groups)
+            *n_groups = (int64_t)op->groups.size();
+        return FPG_OK;
+    }
+
+    int fpg_sparse_repr(const char *string, int32_t n_qubits, uint64_t *cols, void *vals, void *stream)
+    {
+        if (!string || !cols || !vals)
+            return set_error(FPG_ERR_INVALID, "null argument");
+        if (n_qubits < 1 || n_qubits > 40)
+            return set_error(FPG_ERR_UNSUPPORTED, "n_qubits must be in [1, 40]");
+        std::vector<StringRec> recs;
+        std::vector<int32_t> orig;
+        std::vector<Group> groups;
+        std::vector<Chunk> chunks;
+        std::vector<int> cb;
+        int rc = encode_strings(string, 1, n_qubits, recs, orig, groups, chunks, cb);
+        if (rc != FPG_OK)
+            return rc;
+        FPG_CUDA(launch_sparse_repr(recs[0].x, recs[0].z, (int)(recs[0].meta & 3u), n_qubits, cols, vals,
+                                    (cudaStream_t)stream));
+        return FPG_OK;
+    }
+
+    int fpg_expect_strings(const fpg_operator *op, const void *states, double *ev, int64_t n_states, int32_t dtype,
+                           void *stream)
+    {
+        if (!op)
+            return set_error(FPG_ERR_INVALID, "op is null");
+        if (int rc = check_dtype(dtype))
+            return rc;
+        if (n_states < 0)
+            return set_error(FPG_ERR_INVALID, "n_states must be >= 0");
+        if (n_states > 0 && op->P > 0 && (!states || !ev))
+            return set_error(FPG_ERR_INVALID, "null array");
+        if (int rc = check_aligned(dtype, {states}))
+            return rc;
+        if ((uintptr_t)ev % 8 != 0)
+            return set_error(FPG_ERR_INVALID, "ev must be 8-byte aligned");
+        DeviceGuard g(op->device);
+        if (!g.ok)
+            return set_error(FPG_ERR_CUDA, "cannot select the operator's device");
+        return run_expect_strings(op, states, ev, n_states, dtype == FPG_C64, (cudaStream_t)stream);
+    }
+
+    int fpg_summed_expect(const fpg_operator *op, const void *coeffs, int64_t n_operators, const void *states,
+                          void *out, int64_t n_states, int32_t dtype, void *stream)
+    {
+        if (!op)
+            return set_error(FPG_ERR_INVALID, "op is null");
+        if (int rc = check_dtype(dtype))
+            return rc;
+        if (n_states < 0 || n_operators < 0)
+            return set_error(FPG_ERR_INVALID, "n_states and n_operators must be >= 0");
+        if (n_states == 0 || n_operators == 0 || op->P == 0)
+            return FPG_OK;
+        if (!coeffs || !states || !out)
+            return set_error(FPG_ERR_INVALID, "null array");
+        if (int rc = check_aligned(dtype, {coeffs, states, out}))
+            return rc;
+        DeviceGuard g(op->device);
+        if (!g.ok)
+            return set_error(FPG_ERR_CUDA, "cannot select the operator's device");
+        cudaStream_t st = (cudaStream_t)stream;
+        const bool fp32 = dtype == FPG_C64;
+        Scratch evb(st);
+        FPG_CUDA(evb.alloc((size_t)op->P * (size_t)n_states * sizeof(double)));
+        if (int rc = run_expect_strings(op, states, (double *)evb.p, n_states, fp32, st))
+            return rc;
+        FPG_CUDA(launch_contract_real(fp32, coeffs, fp32, (const double *)evb.p, op->P, n_operators, n_states, out,
+                                      st));
+        return FPG_OK;
+    }
+
+    int fpg_apply(const fpg_operator *op, const void *coeffs, const void *states, void *out, int64_t n_states,
+                  int32_t dtype, void *stream)
+    {
+        if (!op)
+            return set_error(FPG_ERR_INVALID, "op is null");
+        if (int rc = check_dtype(dtype))
+            return rc;
+        if (n_states < 0)
+            return set_error(FPG_ERR_INVALID, "n_states must be >= 0");
+        if (n_states == 0 || op->P == 0)
+            return FPG_OK;
+        if (!coeffs || !states || !out)
+            return set_error(FPG_ERR_INVALID, "null array");
+        if (int rc = check_aligned(dtype, {coeffs, states, out}))
+            return rc;
+        DeviceGuard g(op->device);
+        if (!g.ok)
+            return set_error(FPG_ERR_CUDA, "cannot select the operator's device");
+        cudaStream_t st = (cudaStream_t)stream;
+        const bool fp32 = dtype == FPG_C64;
+        const size_t csz = fp32 ? 8 : 16;
+        Scratch cw(st);
+        FPG_CUDA(cw.alloc((size_t)op->P * csz));
+        const DevOp dop = op->dev();
+        FPG_CUDA(launch_prep_coeffs(fp32, dop, coeffs, 0, cw.p, st));
+        FPG_CUDA(launch_apply(fp32, false, dop, cw.p, states, out, n_states, st));
+        return FPG_OK;
+    }
+
+    int fpg_summed_apply(const fpg_operator *op, const void *coeffs, int64_t n_operators, const void *states,
+                         void *out, int64_t n_states, int32_t dtype, void *stream)
+    {
+        if (!op)
+            return set_error(FPG_ERR_INVALID, "op is null");
+        if (int rc = check_dtype(dtype))
+            return rc;
+        if (n_states < 0 || n_operators < 0)
+            return set_error(FPG_ERR_INVALID, "n_states and n_operators must be >= 0");
+        if (n_states == 0 || op->P == 0 || n_operators == 0)
+            return FPG_OK;
+        if (!coeffs || !states || !out)
+            return set_error(FPG_ERR_INVALID, "null array");
+        if (int rc = check_aligned(dtype, {coeffs, states, out}))
+            return rc;
+        DeviceGuard g(op->device);
+        if (!g.ok)
+            return set_error(FPG_ERR_CUDA, "cannot select the operator's device");
+        cudaStream_t st = (cudaStream_t)stream;
+        const bool fp32 = dtype == FPG_C64;
+        const size_t csz = fp32 ? 8 : 16;
+        Scratch cw(st);
+        FPG_CUDA(cw.alloc((size_t)op->P * csz));
+        const DevOp dop = op->dev();
+        FPG_CUDA(launch_prep_coeffs(fp32, dop, coeffs, n_operators, cw.p, st));
+        FPG_CUDA(launch_apply(fp32, false, dop, cw.p, states, out, n_states, st));
+        return FPG_OK;
+    }
+
+    int fpg_summed_apply_weighted(const fpg_operator *op, const void *coeffs, int64_t n_operators,
+                                  const void *states, const void *data, void *out, int64_t n_states, int32_t dtype,
+                                  void *stream)
+    {
+        if (!op)
+            return set_error(FPG_ERR_INVALID, "op is null");
+        if (int rc = check_dtype(dtype))
+            return rc;
+        if (n_states < 0 || n_operators < 0)
+            return set_error(FPG_ERR_INVALID, "n_states and n_operators must be >= 0");
+        if (n_states == 0 || op->P == 0 || n_operators == 0)
+            return FPG_OK;
+        if (!coeffs || !states || !out || !data)
+            return set_error(FPG_ERR_INVALID, "null array");
+        if (int rc = check_aligned(dtype, {coeffs, states, out}))
+            return rc;
+        DeviceGuard g(op->device);
+        if (!g.ok)
+            return set_error(FPG_ERR_CUDA, "cannot select the operator's device");
+        cudaStream_t st = (cudaStream_t)stream;
+        const bool fp32 = dtype == FPG_C64;
+        const size_t csz = fp32 ? 8 : 16;
+        const DevOp dop = op->dev();
+        Scratch w(st), cw(st);
+        FPG_CUDA(w.alloc((size_t)op->P * (size_t)n_states * csz));
+        FPG_CUDA(cw.alloc((size_t)op->P * (size_t)n_states * csz));
+        FPG_CUDA(launch_weighted_coeffs(fp32, coeffs, data, op->P, n_operators, n_states, w.p, st));
+        FPG_CUDA(launch_prep_weighted(fp32, dop, w.p, n_states, cw.p, st));
+        FPG_CUDA(launch_apply(fp32, true, dop, cw.p, states, out, n_states, st));
+        return FPG_OK;
+    }
+
+} // extern "C"

@@ -1,0 +1,117 @@
+// common.cuh -- shared declarations of the GB300 Pauli engine (internal).
+//
+// Encoding.  Pauli string character q (0 = leftmost) acts on row-index bit
+// (n-1-q).  A string is (x, z, nY) with
+//   x = bits of X and Y factors, z = bits of Y and Z factors, nY = #Y,
+// so that its matrix has exactly one non-zero per row:
+//   column(i) = i ^ x,   value(i) = (-i)^nY * (-1)^popcount(i & z).
+// This is the closed form of the reference's get_sparse_repr
+// (fast_pauli/cpp/include/__pauli_string.hpp:49-118).
+//
+// Strings are sorted by x ("x-groups"): every string of a group pairs row i
+// with the same row i ^ x, so one load of the row pair serves the whole group.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fpg
+{
+
+// One Pauli string in sorted (x, parity of nY, z) order; 24 bytes.
+struct StringRec
+{
+    uint64_t x;
+    uint64_t z;
+    uint32_t mask_lo; // bit r (r < 32) = parity(popcount(r & z & 31))
+    uint32_t meta;    // bits 0..1: nY mod 4; bits 8..31 unused
+};
+
+// Original (caller-order) index of each sorted string is kept separately.
+
+// Work unit of the expectation kernel: up to a class maximum of strings of one
+// x-group, n_even strings with even nY at sorted positions
+// [begin_even, begin_even + n_even) and n_odd strings with odd nY at
+// [begin_odd, begin_odd + n_odd).
+struct Chunk
+{
+    uint64_t x;
+    int32_t begin_even;
+    int32_t begin_odd;
+    int16_t n_even;
+    int16_t n_odd;
+    int32_t pad;
+};
+
+struct Group
+{
+    uint64_t x;
+    int32_t begin;
+    int32_t count;
+};
+
+// Device-side view of an encoded operator.
+struct DevOp
+{
+    int n;
+    int64_t P;
+    int64_t G;
+    const StringRec *recs; // [P] sorted
+    const int32_t *orig;   // [P] sorted position -> caller index
+    const Group *groups;   // [G]
+};
+
+// ---------------------------------------------------------------------------
+// launchers (implemented in k_*.cu); all enqueue on `st` and return the
+// cudaError_t of the launch.
+// ---------------------------------------------------------------------------
+
+// Chunk classes of the expectation kernel: (max even strings, max odd strings).
+constexpr int kNumChunkClasses = 8;
+struct ChunkClass
+{
+    int ge, go;
+};
+extern const ChunkClass kChunkClasses[kNumChunkClasses];
+int chunk_class_for(int n_even, int n_odd); // smallest class covering, -1 if none
+
+struct ExpectPlan
+{
+    int TC;           // column lanes per CTA (power of two <= 32)
+    int V;            // complex elements per lane (1 or 2)
+    int n_ctiles;     // column tiles
+    int n_splits;     // row splits (>1 -> partial buffer + reduction)
+};
+
+// ev_or_partial: [n_splits][P][S] float64 (row-major).  One launch per class.
+cudaError_t launch_expect_chunks(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const Chunk *d_chunks,
+                                 int n_chunks, int cls, const ExpectPlan &plan, double *ev_or_partial,
+                                 cudaStream_t st);
+cudaError_t launch_reduce_splits(const double *partial, int n_splits, int64_t count, double *ev, cudaStream_t st);
+
+// out(K,S) += H^T(K,P) * E(P,S); H complex (P,K), E real float64 (P,S).
+// out complex128 (fp32=false) or complex64 (fp32=true).
+cudaError_t launch_contract_real(bool out_c64, const void *H, bool h_c64, const double *E, int64_t P, int64_t K,
+                                 int64_t S, void *out, cudaStream_t st);
+
+// W(P,S) complex = H(P,K) complex * X(K,S) real.  Overwrites W.  Precision by fp32.
+cudaError_t launch_weighted_coeffs(bool fp32, const void *H, const void *X, int64_t P, int64_t K, int64_t S, void *W,
+                                   cudaStream_t st);
+
+// cw_sorted[s] = coeffs[orig[s]] * (-i)^nY   (complex, dtype of coeffs), coeffs: [P] or
+// row sums of (P,K) when K > 0.
+cudaError_t launch_prep_coeffs(bool fp32, const DevOp &op, const void *coeffs, int64_t K, void *cw_sorted,
+                               cudaStream_t st);
+
+// out(D,S) += sum_g psi[i^x_g] * sum_{j in g} cw[j] * (-1)^popc(i & z_j).
+// weighted: cw is (P_sorted, S) complex per column (already * phase, sorted order).
+cudaError_t launch_apply(bool fp32, bool weighted, const DevOp &op, const void *cw, const void *psi, void *out,
+                         int64_t S, cudaStream_t st);
+
+// W(P,S) in caller order -> sorted order with phase: cw[s,t] = W[orig[s],t] * (-i)^nY
+cudaError_t launch_prep_weighted(bool fp32, const DevOp &op, const void *W, int64_t S, void *cw_sorted,
+                                 cudaStream_t st);
+
+cudaError_t launch_sparse_repr(uint64_t x, uint64_t z, int ny, int n, uint64_t *cols, void *vals, cudaStream_t st);
+
+} // namespace fpg

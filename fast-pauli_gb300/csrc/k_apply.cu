@@ -1,0 +1,225 @@
+// k_apply.cu -- apply kernels and their coefficient preparation, and the
+// device sparse pattern.
+//
+// Replaces PauliString::apply_batch (fast_pauli/cpp/include/__pauli_string.hpp:378-436),
+// PauliOp::apply (__pauli_op.hpp:399-468), SummedPauliOp::apply
+// (__summed_pauli_op.hpp:277-349) and the per-string loop of
+// SummedPauliOp::apply_weighted (__summed_pauli_op.hpp:441-455).
+//
+// With strings grouped by x, the operator is sum_g D_g X_g where X_g permutes
+// rows (i -> i^x_g) and D_g is diagonal:
+//     (D_g)_ii = sum_{j in g} c_j (-i)^{nY_j} (-1)^popc(i & z_j).
+// Each output element is written once (no per-thread copies of the output as
+// in the reference, __pauli_op.hpp:427): a thread owns (row i, V columns),
+// walks the groups in a fixed order and accumulates
+//     out(i,t) += sum_g (D_g)_ii psi(i^x_g, t).
+// For apply_weighted the diagonal also depends on the column:
+// w(j,t) (-i)^{nY_j} replaces c_j (-i)^{nY_j}.
+#include "common.cuh"
+
+namespace fpg
+{
+namespace
+{
+
+template <typename T> struct C2;
+template <> struct C2<double>
+{
+    using type = double2;
+};
+template <> struct C2<float>
+{
+    using type = float2;
+};
+
+// multiply by (-i)^ny
+template <typename CT> __device__ __forceinline__ CT times_phase(CT c, int ny)
+{
+    CT r;
+    switch (ny & 3)
+    {
+    case 0: r.x = c.x; r.y = c.y; break;
+    case 1: r.x = c.y; r.y = -c.x; break;   // * (-i)
+    case 2: r.x = -c.x; r.y = -c.y; break;  // * (-1)
+    default: r.x = -c.y; r.y = c.x; break;  // * (+i)
+    }
+    return r;
+}
+
+template <typename CT>
+__global__ void k_prep_coeffs(const StringRec *__restrict__ recs, const int32_t *__restrict__ orig, int64_t P,
+                              const CT *__restrict__ coeffs, int64_t K, CT *__restrict__ cw)
+{
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= P)
+        return;
+    const int64_t j = orig[s];
+    CT c;
+    if (K <= 0)
+        c = coeffs[j];
+    else
+    {
+        // row sum over operators, in the reference's order (__summed_pauli_op.hpp:312-317)
+        c.x = 0;
+        c.y = 0;
+        for (int64_t k = 0; k < K; ++k)
+        {
+            const CT h = coeffs[j * K + k];
+            c.x += h.x;
+            c.y += h.y;
+        }
+    }
+    cw[s] = times_phase(c, (int)(recs[s].meta & 3u));
+}
+
+template <typename CT>
+__global__ void k_prep_weighted(const StringRec *__restrict__ recs, const int32_t *__restrict__ orig, int64_t P,
+                                const CT *__restrict__ W, int64_t S, CT *__restrict__ cw)
+{
+    const int64_t total = P * S;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int64_t s = e / S, t = e - s * S;
+        cw[e] = times_phase(W[(int64_t)orig[s] * S + t], (int)(recs[s].meta & 3u));
+    }
+}
+
+template <typename T, bool WEIGHTED>
+__global__ void __launch_bounds__(256)
+    k_apply(const T *__restrict__ psi, T *__restrict__ out, int64_t S, int n, const Group *__restrict__ groups,
+            int64_t G, const StringRec *__restrict__ recs, const typename C2<T>::type *__restrict__ cw, int TC)
+{
+    using CT = typename C2<T>::type;
+    const int tid = threadIdx.x;
+    const int tc = tid & (TC - 1);
+    const int tr = tid / TC;
+    const int TR = blockDim.x / TC;
+    const uint64_t D = 1ull << n;
+    const uint64_t i = (uint64_t)blockIdx.x * TR + tr;
+    const int64_t t = (int64_t)blockIdx.y * TC + tc;
+    if (i >= D || t >= S)
+        return;
+    const CT *ps = reinterpret_cast<const CT *>(psi);
+    T accr = 0, acci = 0;
+    for (int64_t g = 0; g < G; ++g)
+    {
+        const Group gr = groups[g];
+        T wr = 0, wi = 0;
+        for (int32_t s = gr.begin; s < gr.begin + gr.count; ++s)
+        {
+            const uint64_t z = recs[s].z;
+            const CT c = WEIGHTED ? cw[(int64_t)s * S + t] : cw[s];
+            if (__popcll(i & z) & 1)
+            {
+                wr -= c.x;
+                wi -= c.y;
+            }
+            else
+            {
+                wr += c.x;
+                wi += c.y;
+            }
+        }
+        const CT b = __ldg(ps + (int64_t)(i ^ gr.x) * S + t);
+        accr = fma(wr, b.x, fma(-wi, b.y, accr));
+        acci = fma(wr, b.y, fma(wi, b.x, acci));
+    }
+    CT *o = reinterpret_cast<CT *>(out) + (int64_t)i * S + t;
+    CT cur = *o;
+    cur.x += accr;
+    cur.y += acci;
+    *o = cur;
+}
+
+__global__ void k_sparse_repr(uint64_t x, uint64_t z, int ny, uint64_t D, uint64_t *__restrict__ cols,
+                              double2 *__restrict__ vals)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (uint64_t)gridDim.x * blockDim.x)
+    {
+        cols[i] = i ^ x;
+        double2 one = make_double2((__popcll(i & z) & 1) ? -1.0 : 1.0, 0.0);
+        vals[i] = times_phase(one, ny);
+    }
+}
+
+int pick_tc(int64_t S)
+{
+    int tc = 1;
+    while (tc < 32 && tc < S)
+        tc <<= 1;
+    return tc;
+}
+
+} // namespace
+
+cudaError_t launch_prep_coeffs(bool fp32, const DevOp &op, const void *coeffs, int64_t K, void *cw, cudaStream_t st)
+{
+    if (op.P <= 0)
+        return cudaSuccess;
+    const unsigned blocks = (unsigned)((op.P + 255) / 256);
+    if (fp32)
+        k_prep_coeffs<float2><<<blocks, 256, 0, st>>>(op.recs, op.orig, op.P, (const float2 *)coeffs, K,
+                                                      (float2 *)cw);
+    else
+        k_prep_coeffs<double2><<<blocks, 256, 0, st>>>(op.recs, op.orig, op.P, (const double2 *)coeffs, K,
+                                                       (double2 *)cw);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prep_weighted(bool fp32, const DevOp &op, const void *W, int64_t S, void *cw, cudaStream_t st)
+{
+    if (op.P <= 0 || S <= 0)
+        return cudaSuccess;
+    int64_t blocks = (op.P * S + 255) / 256;
+    if (blocks > 152 * 16)
+        blocks = 152 * 16;
+    const unsigned grid = (unsigned)blocks;
+    if (fp32)
+        k_prep_weighted<float2><<<grid, 256, 0, st>>>(op.recs, op.orig, op.P, (const float2 *)W, S, (float2 *)cw);
+    else
+        k_prep_weighted<double2><<<grid, 256, 0, st>>>(op.recs, op.orig, op.P, (const double2 *)W, S,
+                                                       (double2 *)cw);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_apply(bool fp32, bool weighted, const DevOp &op, const void *cw, const void *psi, void *out,
+                         int64_t S, cudaStream_t st)
+{
+    if (S <= 0 || op.G <= 0)
+        return cudaSuccess;
+    const int TC = pick_tc(S);
+    const int TR = 256 / TC;
+    const uint64_t D = 1ull << op.n;
+    dim3 grid((unsigned)((D + TR - 1) / TR), (unsigned)((S + TC - 1) / TC));
+    if (fp32)
+    {
+        if (weighted)
+            k_apply<float, true><<<grid, 256, 0, st>>>((const float *)psi, (float *)out, S, op.n, op.groups, op.G,
+                                                       op.recs, (const float2 *)cw, TC);
+        else
+            k_apply<float, false><<<grid, 256, 0, st>>>((const float *)psi, (float *)out, S, op.n, op.groups, op.G,
+                                                        op.recs, (const float2 *)cw, TC);
+    }
+    else
+    {
+        if (weighted)
+            k_apply<double, true><<<grid, 256, 0, st>>>((const double *)psi, (double *)out, S, op.n, op.groups, op.G,
+                                                        op.recs, (const double2 *)cw, TC);
+        else
+            k_apply<double, false><<<grid, 256, 0, st>>>((const double *)psi, (double *)out, S, op.n, op.groups,
+                                                         op.G, op.recs, (const double2 *)cw, TC);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sparse_repr(uint64_t x, uint64_t z, int ny, int n, uint64_t *cols, void *vals, cudaStream_t st)
+{
+    const uint64_t D = 1ull << n;
+    uint64_t blocks = (D + 255) / 256;
+    if (blocks > 152 * 32)
+        blocks = 152 * 32;
+    k_sparse_repr<<<(unsigned)blocks, 256, 0, st>>>(x, z, ny, D, cols, (double2 *)vals);
+    return cudaGetLastError();
+}
+
+} // namespace fpg

@@ -1,0 +1,112 @@
+"""ctypes binding of the C ABI in include/fpg.h (libfpg.so).
+
+This is the raw drop-in boundary: plain device pointers, sizes and a stream
+handle.  Tests and bench.py call the engine through it with device buffers
+(e.g. torch CUDA tensors' ``data_ptr()``); the Python classes in
+``fast_pauli`` go through the C++ host API instead.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfpg.so")
+
+FPG_OK = 0
+FPG_ERR_INVALID = 1
+FPG_ERR_CUDA = 2
+FPG_ERR_NOMEM = 3
+FPG_ERR_UNSUPPORTED = 4
+FPG_ERR_TIMEOUT = 5
+FPG_ERR_BUSY = 6
+
+FPG_C128 = 0
+FPG_C64 = 1
+
+_lib = None
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int32
+_PI32 = ctypes.POINTER(ctypes.c_int32)
+_PI64 = ctypes.POINTER(ctypes.c_int64)
+
+# name -> (restype, argtypes); mirrors include/fpg.h
+SIGNATURES = {
+    "fpg_abi_version": (ctypes.c_int, []),
+    "fpg_last_error": (ctypes.c_char_p, []),
+    "fpg_device_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int)]),
+    "fpg_pointer_is_device": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
+    "fpg_operator_create": (ctypes.c_int, [ctypes.c_char_p, _I64, _I32, ctypes.POINTER(_P)]),
+    "fpg_operator_destroy": (ctypes.c_int, [_P]),
+    "fpg_operator_info": (ctypes.c_int, [_P, _PI32, _PI64, _PI64]),
+    "fpg_sparse_repr": (ctypes.c_int, [ctypes.c_char_p, _I32, _P, _P, _P]),
+    "fpg_apply": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I32, _P]),
+    "fpg_expect_strings": (ctypes.c_int, [_P, _P, _P, _I64, _I32, _P]),
+    "fpg_summed_expect": (ctypes.c_int, [_P, _P, _I64, _P, _P, _I64, _I32, _P]),
+    "fpg_summed_apply": (ctypes.c_int, [_P, _P, _I64, _P, _P, _I64, _I32, _P]),
+    "fpg_summed_apply_weighted": (ctypes.c_int, [_P, _P, _I64, _P, _P, _P, _I64, _I32, _P]),
+}
+
+
+class FpgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"fpg error {code}: {msg}")
+        self.code = code
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is not built (run __graft_entry__.build())")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name, None)
+            if f is None:
+                continue
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc: int) -> None:
+    if rc != FPG_OK:
+        raise FpgError(rc, lib().fpg_last_error().decode())
+
+
+class Operator:
+    """Owning handle of an fpg_operator (encoded strings on the device)."""
+
+    def __init__(self, strings: list[str]):
+        strings = [str(s) for s in strings]
+        n = len(strings[0]) if strings else 1
+        self.n_qubits = n
+        self.n_strings = len(strings)
+        self._h = _P()
+        check(lib().fpg_operator_create("".join(strings).encode(), len(strings), n, ctypes.byref(self._h)))
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def info(self) -> tuple[int, int, int]:
+        n = ctypes.c_int32()
+        p = ctypes.c_int64()
+        g = ctypes.c_int64()
+        check(lib().fpg_operator_info(self._h, ctypes.byref(n), ctypes.byref(p), ctypes.byref(g)))
+        return n.value, p.value, g.value
+
+    def close(self) -> None:
+        if self._h:
+            lib().fpg_operator_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

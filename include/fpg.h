@@ -1,0 +1,144 @@
+/*
+ * fpg.h -- C ABI of the GB300 Pauli apply / expectation engine (libfpg.so).
+ *
+ * This is the drop-in boundary for the hot path of qognitive/fast-pauli:
+ * PauliString / PauliOp / SummedPauliOp apply, apply_weighted and
+ * expectation_value.  The reference's bindings call its header-only C++
+ * templates directly (fast_pauli/cpp/src/include/__*_bindings.hpp); here the
+ * C++ host classes (fast-pauli_gb300/cpp/include/fast_pauli_gb300.hpp) and the
+ * Python module fast_pauli._fast_pauli call these entry points instead.
+ *
+ * Conventions
+ *  - Every function returns an int status: FPG_OK (0) or an FPG_ERR_* code;
+ *    nothing aborts.  fpg_last_error() gives the message of the calling
+ *    thread's last failure.  Argument errors map to the reference's
+ *    std::invalid_argument (Python ValueError).
+ *  - Array arguments are DEVICE pointers owned by the caller, row-major.
+ *    States are (2^n_qubits, n_states): states are columns, the state index is
+ *    the fastest-varying, exactly the reference's layout.
+ *  - Outputs ACCUMULATE (+=) like the reference (e.g.
+ *    fast_pauli/cpp/include/__pauli_string.hpp:338,432,534,
+ *    __summed_pauli_op.hpp:609): callers zero them first.
+ *  - Work is ordered on `stream` (a cudaStream_t, NULL = legacy default
+ *    stream); functions return once the work is enqueued.  Scratch memory is
+ *    drawn from the device's stream-ordered pool (cudaMallocAsync).
+ *  - dtype FPG_C128: complex128 data, float64 arithmetic (the reference's
+ *    precision).  dtype FPG_C64: complex64 data, float32 arithmetic with
+ *    compensated float32 partial sums, float64 cross-block reduction, 3xTF32
+ *    tensor-core coefficient contraction.
+ *  - Pauli strings are passed as characters 'I','X','Y','Z', n_qubits
+ *    characters per string, concatenated.  The leftmost character acts on the
+ *    most significant bit of the row index (reference: __pauli_string.hpp:54).
+ */
+#ifndef FPG_H
+#define FPG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FPG_ABI_VERSION 1
+
+enum fpg_status
+{
+    FPG_OK = 0,
+    FPG_ERR_INVALID = 1,     /* bad argument: shapes, characters, null pointers  */
+    FPG_ERR_CUDA = 2,        /* a CUDA runtime call failed                        */
+    FPG_ERR_NOMEM = 3,       /* device or host allocation failed                  */
+    FPG_ERR_UNSUPPORTED = 4, /* e.g. n_qubits beyond the supported range          */
+    FPG_ERR_TIMEOUT = 5,     /* a bounded device wait gave up                     */
+    FPG_ERR_BUSY = 6         /* admission refused (serving loop)                  */
+};
+
+enum fpg_dtype
+{
+    FPG_C128 = 0,
+    FPG_C64 = 1
+};
+
+/* Opaque, device-resident encoding of a list of Pauli strings:
+ * per string (x mask, z mask, #Y), grouped by x mask. */
+typedef struct fpg_operator fpg_operator;
+
+/* ABI version (FPG_ABI_VERSION). */
+int fpg_abi_version(void);
+
+/* Message for the calling thread's most recent failure ("" if none). */
+const char *fpg_last_error(void);
+
+/* Number of visible CUDA devices (0 on a machine without a GPU). */
+int fpg_device_count(int *count);
+
+/* 1 if ptr is device (or managed) memory on some device, else 0. */
+int fpg_pointer_is_device(const void *ptr, int *is_device);
+
+/*
+ * Encode n_strings Pauli strings of n_qubits characters each and upload the
+ * encoding to the current device.  Replaces the per-call get_sparse_repr of
+ * the reference (__pauli_string.hpp:49-118), which the reference rebuilds for
+ * every string on every apply/expectation call.  Raises FPG_ERR_INVALID on a
+ * character outside IXYZ (reference: PauliString(std::string),
+ * __pauli_string.hpp:193-194).  1 <= n_qubits <= 40.
+ */
+int fpg_operator_create(const char *strings, int64_t n_strings, int32_t n_qubits, fpg_operator **out);
+int fpg_operator_destroy(fpg_operator *op);
+int fpg_operator_info(const fpg_operator *op, int32_t *n_qubits, int64_t *n_strings, int64_t *n_groups);
+
+/*
+ * Sparse pattern of one Pauli string on the device: cols[i] = column of the
+ * non-zero in row i, vals[i] = its value (complex128 interleaved), i < 2^n.
+ * Bit-exact replacement for get_sparse_repr<double>
+ * (__pauli_string.hpp:49-118; Python helpers.pauli_string_sparse_repr,
+ * fast_pauli/cpp/src/fast_pauli.cpp:92).
+ */
+int fpg_sparse_repr(const char *string, int32_t n_qubits, uint64_t *cols, void *vals, void *stream);
+
+/*
+ * out(D,S) += sum_j coeffs[j] * P_j * states        (coeffs: n_strings complex)
+ * Replaces PauliOp::apply (__pauli_op.hpp:399-468) and, with one string,
+ * PauliString::apply_batch (__pauli_string.hpp:378-436).
+ */
+int fpg_apply(const fpg_operator *op, const void *coeffs, const void *states, void *out, int64_t n_states,
+              int32_t dtype, void *stream);
+
+/*
+ * Per-string expectation values ev(j,t) = <psi_t| P_j |psi_t> (real; Pauli
+ * strings are Hermitian), float64, shape (n_strings, n_states); ev is
+ * OVERWRITTEN.  The per-string stage of SummedPauliOp::expectation_value
+ * (__summed_pauli_op.hpp:572-577) and of PauliString::expectation_value
+ * (__pauli_string.hpp:471-538).
+ */
+int fpg_expect_strings(const fpg_operator *op, const void *states, double *ev, int64_t n_states, int32_t dtype,
+                       void *stream);
+
+/*
+ * out(K,S) += sum_j coeffs(j,k) * <psi_t|P_j|psi_t>   (coeffs: (n_strings, K) complex)
+ * Replaces SummedPauliOp::expectation_value (__summed_pauli_op.hpp:520-614);
+ * with K = 1 it is PauliOp::expectation_value (__pauli_op.hpp:482-549).
+ */
+int fpg_summed_expect(const fpg_operator *op, const void *coeffs, int64_t n_operators, const void *states, void *out,
+                      int64_t n_states, int32_t dtype, void *stream);
+
+/*
+ * out(D,S) += sum_j (sum_k coeffs(j,k)) P_j states
+ * Replaces SummedPauliOp::apply (__summed_pauli_op.hpp:277-349).
+ */
+int fpg_summed_apply(const fpg_operator *op, const void *coeffs, int64_t n_operators, const void *states, void *out,
+                     int64_t n_states, int32_t dtype, void *stream);
+
+/*
+ * out(:,t) += sum_j w(j,t) P_j states(:,t),  w(j,t) = sum_k coeffs(j,k) data(k,t)
+ * data is real, shape (K, S): float64 for FPG_C128, float32 for FPG_C64.
+ * Replaces SummedPauliOp::apply_weighted (__summed_pauli_op.hpp:365-503).
+ */
+int fpg_summed_apply_weighted(const fpg_operator *op, const void *coeffs, int64_t n_operators, const void *states,
+                              const void *data, void *out, int64_t n_states, int32_t dtype, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FPG_H */

@@ -1,0 +1,276 @@
+"""GPU parity: the CUDA path against the reference's golden outputs and the CPU
+oracle on the same seeded inputs (float64 path within 1e-12 normwise relative;
+index/sign/phase work bit-exact), plus size-independent properties at the
+full configuration-2 size.  Everything runs through libfpg's C ABI: via the
+Python module (C++ host API -> C ABI) or directly via ctypes."""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import TOL_C128, TOL_MIXED, golden, normwise
+
+pytestmark = pytest.mark.gpu
+
+fp = pytest.importorskip("fast_pauli")
+
+
+def _strs(a):
+    return [str(x) for x in a]
+
+
+# ---------------------------------------------------------------- goldens
+
+
+def test_sparse_repr_bit_exact_vs_reference():
+    g = golden("sparse_repr.npz")
+    for s in _strs(g["strings"]):
+        cols, vals = fp.helpers.pauli_string_sparse_repr([fp.Pauli(c) for c in s])
+        np.testing.assert_array_equal(np.array(cols, dtype=np.uint64), g[f"cols_{s}"])
+        np.testing.assert_array_equal(np.array(vals), g[f"vals_{s}"])
+
+
+def test_config1_pauli_op_apply_vs_reference():
+    g = golden("config1_pauli_op_apply.npz")
+    got = fp.PauliOp(g["coeffs"], _strs(g["strings"])).apply(g["states"])
+    assert got.shape == (1024, 100) and got.dtype == np.complex128
+    assert normwise(got, g["out"]) < TOL_C128
+
+
+def test_small_methods_vs_reference():
+    g = golden("small_methods.npz")
+    s = _strs(g["strings"])
+    c = complex(g["c"])
+    psi, psi1 = g["states"], g["state1"]
+    sop = fp.SummedPauliOp(s, g["h"])
+    got = {
+        "string_apply_2d": fp.PauliString(s[0]).apply(psi, c),
+        "string_apply_1d": fp.PauliString(s[0]).apply(psi1, c),  # 1-D ignores coeff, as the reference
+        "string_expectation": fp.PauliString(s[1]).expectation_value(psi, c),
+        "op_apply": fp.PauliOp(g["coeffs"], s).apply(psi),
+        "op_expectation": fp.PauliOp(g["coeffs"], s).expectation_value(psi),
+        "summed_expectation": sop.expectation_value(psi),
+        "summed_apply": sop.apply(psi),
+        "summed_apply_weighted": sop.apply_weighted(psi, g["data"]),
+    }
+    for k, v in got.items():
+        assert v.shape == g[k].shape, k
+        assert normwise(v, g[k]) < TOL_C128, (k, normwise(v, g[k]))
+
+
+def test_config2_reduced_vs_reference():
+    g = golden("config2_reduced_summed_expectation.npz")
+    got = fp.SummedPauliOp(_strs(g["strings"]), g["h"]).expectation_value(g["states"])
+    assert normwise(got, g["out"]) < TOL_C128
+
+
+# ------------------------------------------------------ seeded oracle sweeps
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 6, 7, 9])
+@pytest.mark.parametrize("S", [1, 3, 32, 37])
+def test_uniform_strings_all_methods(n, S):
+    rng = np.random.default_rng(100 * n + S)
+    P, K = 2 + 3 * n, 3
+    strings = oracle.uniform_strings(rng, n, P)
+    coeffs = rng.standard_normal(P) + 1j * rng.standard_normal(P)
+    h = rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    data = rng.standard_normal((K, S))
+    op = fp.PauliOp(coeffs, strings)
+    sop = fp.SummedPauliOp(strings, h)
+    assert normwise(op.apply(psi), oracle.op_apply(strings, coeffs, psi)) < TOL_C128
+    assert normwise(op.expectation_value(psi), oracle.op_expectation(strings, coeffs, psi)) < TOL_C128
+    assert normwise(sop.expectation_value(psi), oracle.summed_expectation(strings, h, psi)) < TOL_C128
+    assert normwise(sop.apply(psi), oracle.summed_apply(strings, h, psi)) < TOL_C128
+    assert normwise(sop.apply_weighted(psi, data), oracle.summed_apply_weighted(strings, h, psi, data)) < TOL_C128
+
+
+@pytest.mark.parametrize("n", [5, 6, 8, 11])
+@pytest.mark.parametrize("S", [1, 16, 40])
+def test_weight2_strings_summed_expectation(n, S):
+    # the configuration-2 string set (all weight <= 2 strings minus the
+    # identity): large x-groups, mixed #Y parities, paired and unpaired rows
+    rng = np.random.default_rng(7 * n + S)
+    strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
+    P, K = len(strings), 5
+    h = (rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))) / np.sqrt(2 * P)
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    got = fp.SummedPauliOp(strings, h).expectation_value(psi)
+    assert normwise(got, oracle.summed_expectation(strings, h, psi)) < TOL_C128
+
+
+def test_exhaustive_small_strings_vs_dense():
+    rng = np.random.default_rng(3)
+    for n in (1, 2, 3):
+        psi = oracle.unit_norm_states(rng, 1 << n, 5)
+        for s in oracle.calculate_pauli_strings_max_weight(n, n):
+            d = oracle.dense(s)
+            want = np.einsum("it,ij,jt->t", psi.conj(), d, psi)
+            got = fp.PauliString(s).expectation_value(psi)
+            np.testing.assert_allclose(got, want, atol=1e-14)
+            np.testing.assert_allclose(fp.PauliString(s).apply(psi), d @ psi, atol=1e-14)
+
+
+def test_one_dimensional_and_edge_inputs():
+    rng = np.random.default_rng(4)
+    strings = ["XYZ", "ZZI", "IYX"]
+    coeffs = np.array([1.0, -2j, 0.5])
+    psi = oracle.unit_norm_states(rng, 8, 1)[:, 0].copy()
+    op = fp.PauliOp(coeffs, strings)
+    out = op.apply(psi)
+    assert out.shape == (8,)
+    assert normwise(out, oracle.op_apply(strings, coeffs, psi)) < TOL_C128
+    ev = op.expectation_value(psi)
+    assert ev.shape == (1,)
+    sop = fp.SummedPauliOp(strings, np.ones((3, 2), dtype=complex))
+    assert sop.expectation_value(psi).shape == (2,)
+    w = sop.apply_weighted(psi, np.array([0.5, -1.0]))
+    assert w.shape == (8,)
+    # int / float inputs are converted like the reference's nanobind conversion
+    np.testing.assert_allclose(fp.PauliString("III").apply(np.arange(8)), np.arange(8), atol=1e-15)
+    np.testing.assert_allclose(fp.PauliString("IXYZ").apply(np.zeros((16, 16))), np.zeros((16, 16)), atol=0)
+    # zero states
+    assert fp.PauliOp(coeffs, strings).apply(np.zeros((8, 0), dtype=complex)).shape == (8, 0)
+    # non-C-contiguous complex128 input -> ValueError (reference __nb_helpers.hpp:55-74)
+    with pytest.raises(ValueError):
+        op.apply(np.asfortranarray(oracle.unit_norm_states(rng, 8, 4)))
+    # shape errors (reference test_pauli_op.py:936-946)
+    with pytest.raises(ValueError):
+        fp.PauliOp([1, 1, 1], ["X", "Y", "Z"]).apply(np.ones(3))
+    with pytest.raises(ValueError):
+        fp.PauliOp([1, 1, 1], ["X", "Y", "Z"]).apply(np.eye(4))
+    with pytest.raises(ValueError):
+        fp.PauliOp([1, 1], ["XYZ", "ZYX"]).expectation_value(np.ones(32))
+    with pytest.raises(ValueError):
+        fp.PauliOp([1, 1], ["XYZ", "ZYX"]).expectation_value(np.eye(16))
+    with pytest.raises(ValueError):
+        sop.apply_weighted(np.ones((8, 3)), np.ones((3, 3)))
+
+
+def test_duplicate_strings_and_identity():
+    rng = np.random.default_rng(8)
+    strings = ["XX", "XX", "II", "ZY", "II"]
+    coeffs = rng.standard_normal(5) + 1j * rng.standard_normal(5)
+    psi = oracle.unit_norm_states(rng, 4, 6)
+    op = fp.PauliOp(coeffs, strings)
+    assert normwise(op.apply(psi), oracle.op_apply(strings, coeffs, psi)) < TOL_C128
+    assert normwise(op.expectation_value(psi), oracle.op_expectation(strings, coeffs, psi)) < TOL_C128
+
+
+def test_to_tensor_matches_dense():
+    rng = np.random.default_rng(2)
+    strings = oracle.uniform_strings(rng, 3, 5)
+    c = rng.standard_normal(5) + 1j * rng.standard_normal(5)
+    want = sum(ci * oracle.dense(s) for ci, s in zip(c, strings))
+    np.testing.assert_allclose(fp.PauliOp(c, strings).to_tensor(), want, atol=1e-14)
+    np.testing.assert_allclose(fp.PauliString("XYZ").to_tensor(), oracle.dense("XYZ"), atol=0)
+    h = np.stack([c, 2 * c], axis=1)
+    t = fp.SummedPauliOp(strings, h).to_tensor()
+    np.testing.assert_allclose(t[1], 2 * want, atol=1e-13)
+
+
+# ------------------------------------------------------------ device tensors
+
+
+def test_torch_device_tensors_c128_and_mixed():
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(21)
+    n, S, K = 9, 48, 6
+    strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
+    P = len(strings)
+    h = (rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))) / np.sqrt(2 * P)
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    want = oracle.summed_expectation(strings, h, psi)
+    sop = fp.SummedPauliOp(strings, h)
+    t128 = torch.from_numpy(psi).cuda()
+    got = sop.expectation_value(t128)
+    assert isinstance(got, torch.Tensor) and got.is_cuda and got.dtype == torch.complex128
+    assert normwise(got.cpu().numpy(), want) < TOL_C128
+    t64 = t128.to(torch.complex64)
+    got64 = sop.expectation_value(t64)
+    assert got64.dtype == torch.complex64
+    assert normwise(got64.cpu().numpy(), want) < TOL_MIXED
+    # apply on device, both precisions
+    wa = oracle.summed_apply(strings, h, psi)
+    assert normwise(sop.apply(t128).cpu().numpy(), wa) < TOL_C128
+    assert normwise(sop.apply(t64).cpu().numpy(), wa) < TOL_MIXED
+
+
+# ------------------------------------------------------------ raw C ABI
+
+
+def test_c_abi_direct_device_buffers():
+    torch = pytest.importorskip("torch")
+    from fast_pauli import _abi
+
+    L = _abi.lib()
+    rng = np.random.default_rng(31)
+    n, S, K = 8, 20, 4
+    strings = oracle.uniform_strings(rng, n, 30)
+    P = len(strings)
+    h = rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    op = _abi.Operator(strings)
+    nq, ps, ng = op.info()
+    assert (nq, ps) == (n, P) and 1 <= ng <= P
+    dpsi = torch.from_numpy(psi).cuda()
+    dh = torch.from_numpy(h).cuda()
+    dout = torch.zeros((K, S), dtype=torch.complex128, device="cuda")
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _abi.check(L.fpg_summed_expect(op.handle, dh.data_ptr(), K, dpsi.data_ptr(), dout.data_ptr(), S,
+                                   _abi.FPG_C128, st))
+    # outputs accumulate: a second call doubles the result
+    _abi.check(L.fpg_summed_expect(op.handle, dh.data_ptr(), K, dpsi.data_ptr(), dout.data_ptr(), S,
+                                   _abi.FPG_C128, st))
+    torch.cuda.synchronize()
+    assert normwise(dout.cpu().numpy(), 2 * oracle.summed_expectation(strings, h, psi)) < TOL_C128
+    ev = torch.empty((P, S), dtype=torch.float64, device="cuda")
+    _abi.check(L.fpg_expect_strings(op.handle, dpsi.data_ptr(), ev.data_ptr(), S, _abi.FPG_C128, st))
+    torch.cuda.synchronize()
+    for j in (0, 7, P - 1):
+        want = oracle.string_expectation(strings[j], psi)
+        assert np.abs(ev[j].cpu().numpy() - want.real).max() < 1e-13
+        assert np.abs(want.imag).max() < 1e-13  # Hermitian: expectations are real
+    dtype_bad = L.fpg_summed_expect(op.handle, dh.data_ptr(), K, dpsi.data_ptr(), dout.data_ptr(), S, 7, st)
+    assert dtype_bad == _abi.FPG_ERR_INVALID
+    op.close()
+
+
+# ------------------------------------------- full-size properties (config 2)
+
+
+def test_config2_full_size_properties():
+    """n=14, all 861 weight<=2 strings, S=1024 (the bench workload's shape,
+    K reduced): size-independent properties instead of the oracle."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(1002)
+    n, S = 14, 1024
+    strings = oracle.calculate_pauli_strings_max_weight(n, 2)
+    P = len(strings)  # 862 incl. the identity at index 0
+    psi = torch.from_numpy(oracle.unit_norm_states(rng, 1 << n, S)).cuda()
+    K = 3
+    h1 = rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))
+    h2 = rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))
+    e1 = fp.SummedPauliOp(strings, h1).expectation_value(psi).cpu().numpy()
+    e2 = fp.SummedPauliOp(strings, h2).expectation_value(psi).cpu().numpy()
+    a = 0.3 - 1.7j
+    e12 = fp.SummedPauliOp(strings, a * h1 + h2).expectation_value(psi).cpu().numpy()
+    assert normwise(e12, a * e1 + e2) < 1e-12  # linearity in the coefficients
+    # identity string: <psi|psi> = 1 for unit-norm columns
+    eid = fp.PauliString("I" * n).expectation_value(psi).cpu().numpy()
+    np.testing.assert_allclose(eid, np.ones(S), atol=1e-12)
+    # consistency of two kernels: <psi| (A psi) > == expectation of A
+    coeffs = rng.standard_normal(P) + 1j * rng.standard_normal(P)
+    op = fp.PauliOp(coeffs, strings)
+    applied = op.apply(psi)
+    via_apply = torch.einsum("it,it->t", psi.conj(), applied).cpu().numpy()
+    assert normwise(op.expectation_value(psi).cpu().numpy(), via_apply) < 1e-12
+    # P^2 = I for a single string
+    s = fp.PauliString("XYZI" * 3 + "YZ")
+    back = s.apply(s.apply(psi))
+    assert normwise(back.cpu().numpy(), psi.cpu().numpy()) < 1e-15
