@@ -1,0 +1,460 @@
+"""Benchmark of the Pauli expectation hot path on GB300.
+
+Default workload (one "step"): SummedPauliOp.expectation_value in float64 at
+n = 14 qubits, the 861 strings of weight <= 2 (calculate_pauli_strings_max_weight
+minus the identity), K = 1000 operators with coefficients ~ CN(0, 1/861),
+16384 x 1024 complex128 unit-norm Gaussian states -> (1000, 1024).  Metric:
+amplitude-terms/s = n_strings * 2^n * n_states per second.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank runs its own full workload on its own GPU
+(weak scaling, no data-path collective); only the timing is reduced (max).
+Rank 0 prints one JSON line.
+
+Keys beyond the base contract:
+  roofline      streaming-equivalent bytes (16 B per amplitude-term + coeffs +
+                outputs) of the dominant stage (the per-string expectation
+                kernels, timed alone with CUDA events) vs the measured HBM copy
+                bandwidth; "pipe" gives the same stage's float64 operation rate
+                vs the measured float64 FMA peak.
+  cpu_baseline  the CPU oracle port (OpenMP, all host threads) on a bounded
+                sample of the same workload.
+  mixed         the complex64 / float32 path on the n = 18 shape (1431 strings,
+                K = 1000, 262144 x 512), its throughput and its error against
+                the float64 GPU path.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "fast-pauli_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "expval amplitude-terms/s"
+UNIT = "amplitude-terms/s"
+# float64 FMA throughput of a GB300 measured on this machine with an independent
+# FMA-chain kernel (1.19 TFLOP/s, FMA = 2 FLOP); MEASURED_PEAKS.json has no
+# float64 figure.
+FP64_PEAK_TFLOPS = 1.19
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples during the timed region (median SM clock, reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ workload
+def config2(n=14, K=1000, S=1024, seed=1002, device="cuda"):
+    import numpy as np
+    import torch
+
+    import fast_pauli as fp
+
+    strings = [str(s) for s in fp.helpers.calculate_pauli_strings_max_weight(n, 2)][1:]
+    P = len(strings)
+    rng = np.random.default_rng(seed)
+    sd = np.sqrt(1.0 / (2 * P))
+    h = (rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))) * sd
+    g = torch.Generator(device=device).manual_seed(seed)
+    D = 1 << n
+    psi = torch.complex(torch.randn(D, S, dtype=torch.float64, device=device, generator=g),
+                        torch.randn(D, S, dtype=torch.float64, device=device, generator=g))
+    psi /= torch.linalg.vector_norm(psi, dim=0, keepdim=True)
+    return strings, h, psi
+
+
+def _stream_handle():
+    import torch
+
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def time_device(fn, steps, warmup):
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(steps):
+        fn()
+    e1.record(st)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1000.0 / steps
+
+
+# ------------------------------------------------------------------ arms
+def run_ours(args, rank, world, dist):
+    import numpy as np
+    import torch
+
+    import fast_pauli as fp
+    from fast_pauli import _abi
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    n, K, S = 14, 1000, 1024
+    strings, h, psi = config2(n=n, K=K, S=S, seed=1002 + rank)
+    P, D = len(strings), 1 << n
+    terms = P * D * S
+    L = _abi.lib()
+    op = _abi.Operator(strings)
+    dh = torch.from_numpy(h).cuda()
+    out = torch.zeros((K, S), dtype=torch.complex128, device="cuda")
+    ev = torch.empty((P, S), dtype=torch.float64, device="cuda")
+    stream = _stream_handle()
+
+    def step():
+        out.zero_()
+        _abi.check(L.fpg_summed_expect(op.handle, dh.data_ptr(), K, psi.data_ptr(), out.data_ptr(), S,
+                                       _abi.FPG_C128, stream))
+
+    def expect_stage():
+        _abi.check(L.fpg_expect_strings(op.handle, psi.data_ptr(), ev.data_ptr(), S, _abi.FPG_C128, stream))
+
+    if args.profile:
+        # one-shot case for ncu captures: warm-up then a few launches of the stage
+        for _ in range(max(1, args.warmup)):
+            expect_stage()
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            step()
+        torch.cuda.synchronize()
+        return None
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local) if rank == 0 else None
+    if clocks:
+        clocks.start()
+        time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    n0 = _abi.kernel_launches()
+    st = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(args.steps):
+        step()
+    e1.record(st)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches = _abi.kernel_launches() - n0
+    t_step = e0.elapsed_time(e1) / 1000.0 / args.steps
+    if dist:
+        tt = torch.tensor([t_step], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step = float(tt.item())
+    # dominant stage alone (per-string expectation kernels), same stream
+    t_expect = time_device(expect_stage, args.steps, 2)
+    clk = clocks.stop() if clocks else None
+    if rank != 0:
+        return None
+
+    # result sanity: identity-free strings, Hermitian -> E has the symmetry
+    # E(h) real-linear; check a column against the oracle on a tiny slice
+    hbm, peak_kind = _peaks()
+    e_bytes = 16
+    alg_bytes_expect = terms * e_bytes
+    nch, visits, adds = op.stats()
+    fp64_ops = S * (4 * visits + adds)
+    roof = {
+        "bound": "hbm",
+        "achieved": alg_bytes_expect / t_expect / 1e9,
+        "peak": hbm,
+        "unit": "GB/s",
+        "frac": alg_bytes_expect / t_expect / 1e9 / hbm,
+        "peak_kind": peak_kind,
+        "traffic": _ncu_traffic("k_expect_chunks_config2_fp64.md"),
+        "kernel": "k_expect_chunks (fpg_expect_strings stage)",
+        "kernel_ms": t_expect * 1e3,
+        "algorithmic_bytes_per_launch": alg_bytes_expect,
+        "pipe": {"kind": "fp64", "ops_per_launch": fp64_ops, "achieved_tflops": 2 * fp64_ops / t_expect / 1e12,
+                 "peak_tflops": FP64_PEAK_TFLOPS,
+                 "frac": 2 * fp64_ops / t_expect / 1e12 / FP64_PEAK_TFLOPS,
+                 "note": "FMA-equivalent float64 instructions x2; FP64 pipe bound"},
+    }
+
+    # ---- end to end through the public API, host (pinned) buffers ---------
+    e2e = None
+    if not args.skip_e2e:
+        sop = fp.SummedPauliOp(strings, h)
+        pinned = torch.empty((D, S), dtype=torch.complex128, pin_memory=True)
+        pinned.copy_(psi.cpu())
+        host = pinned.numpy()
+        res = sop.expectation_value(host)  # warm-up (encodes the strings once)
+        ref_dev = out.cpu().numpy()
+        e2e_err = float(np.abs(res - ref_dev).max() / np.abs(ref_dev).max())
+        ksteps = max(3, args.steps // 2)
+        t0 = time.perf_counter()
+        for _ in range(ksteps):
+            res = sop.expectation_value(host)
+        t1 = time.perf_counter()
+        e2e = {"value": world * terms / ((t1 - t0) / ksteps), "unit": UNIT,
+               "h2d_bytes_per_step": D * S * 16 + P * K * 16, "d2h_bytes_per_step": K * S * 16,
+               "api": "fast_pauli.SummedPauliOp.expectation_value(numpy, pinned host memory)",
+               "max_rel_err_vs_device_path": e2e_err}
+
+    # ---- CPU baseline (oracle port, bounded sample) ------------------------
+    cpu = None
+    if not args.skip_cpu and world == 1:
+        cpu = cpu_sample(strings, h, psi, S, n)
+
+    mixed = None
+    if not args.skip_mixed:
+        mixed = run_mixed(args)
+
+    line = {
+        "metric": METRIC, "value": world * terms / t_step, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128/f64", "data": "synthetic (seeded Gaussian unit-norm states)",
+        "config": {"workload": "SummedPauliOp.expectation_value float64: n=14, 861 weight<=2 strings, "
+                               "K=1000, states 16384x1024 complex128",
+                   "n_qubits": n, "n_strings": P, "n_operators": K, "n_states": S,
+                   "l2": "inputs (256 MiB states) larger than L2; no flush",
+                   "parallelism": f"replicas x{world} (columns independent, no collective)"},
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+        "launches_per_step": launches / args.steps, "clocks": clk, "mixed": mixed,
+    }
+    return line
+
+
+def cpu_sample(strings, h, psi, S, n):
+    """Oracle port (the reference's OpenMP algorithm) on a bounded sample:
+    the first 108 of the 861 strings (1/8), all K and all states."""
+    import numpy as np
+
+    import oracle
+
+    sub = 108
+    hs = np.ascontiguousarray(h[:sub])
+    host = psi.cpu().numpy()
+    oracle.summed_expectation(strings[:2], hs[:2], host[:, :8])  # load + warm
+    t0 = time.perf_counter()
+    oracle.summed_expectation(strings[:sub], hs, host)
+    t = time.perf_counter() - t0
+    terms = sub * (1 << n) * S
+    return {"value": terms / t, "unit": UNIT, "cores": oracle.max_threads(), "kind": "port",
+            "sample": f"first {sub} of 861 strings, K=1000, all 16384x1024 states ({t:.2f} s)"}
+
+
+def run_mixed(args):
+    """complex64 / float32 path on the n=18 shape; error vs the float64 GPU path."""
+    import numpy as np
+    import torch
+
+    from fast_pauli import _abi
+
+    n, K, S = 18, 1000, 512
+    strings, h, psi = config2(n=n, K=K, S=S, seed=1003)
+    P, D = len(strings), 1 << n
+    L = _abi.lib()
+    op = _abi.Operator(strings)
+    stream = _stream_handle()
+    h128 = torch.from_numpy(h).cuda()
+    h64 = h128.to(torch.complex64)
+    psi64 = psi.to(torch.complex64)
+    out128 = torch.zeros((K, S), dtype=torch.complex128, device="cuda")
+    out64 = torch.zeros((K, S), dtype=torch.complex64, device="cuda")
+
+    def f128():
+        out128.zero_()
+        _abi.check(L.fpg_summed_expect(op.handle, h128.data_ptr(), K, psi.data_ptr(), out128.data_ptr(), S,
+                                       _abi.FPG_C128, stream))
+
+    def f64():
+        out64.zero_()
+        _abi.check(L.fpg_summed_expect(op.handle, h64.data_ptr(), K, psi64.data_ptr(), out64.data_ptr(), S,
+                                       _abi.FPG_C64, stream))
+
+    t128 = time_device(f128, 2, 1)
+    steps = max(3, args.steps // 2)
+    t64 = time_device(f64, steps, 2)
+    ref = out128.cpu().numpy()
+    got = out64.cpu().numpy().astype(np.complex128)
+    err = np.abs(got - ref)
+    den = np.abs(ref).max()
+    terms = P * D * S
+    del psi, psi64
+    torch.cuda.empty_cache()
+    hbm, _ = _peaks()
+    return {"workload": f"n={n}, {P} strings, K={K}, states {D}x{S} complex64", "terms_per_s": terms / t64,
+            "ms_per_step": t64 * 1e3, "fp64_ms_per_step": t128 * 1e3, "speedup_vs_fp64": t128 / t64,
+            "streaming_equiv_frac_of_hbm": terms * 8 / t64 / 1e9 / hbm,
+            "max_normwise_rel_err_vs_fp64": float(err.max() / den),
+            "mean_rel_err_vs_fp64": float(err.mean() / np.abs(ref).mean())}
+
+
+def _ncu_traffic(summary: str):
+    """DRAM bytes (read + write) of the timed stage from a committed ncu
+    summary under profiles/ (the ``traffic_bytes_per_stage:`` line)."""
+    import re
+
+    try:
+        with open(os.path.join(ROOT, "profiles", summary)) as f:
+            m = re.search(r"traffic_bytes_per_stage:\s*([0-9]+)", f.read())
+        return int(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+def run_reference(args, rank, world):
+    """The reference's own CPU algorithm (oracle/_ref when built from the
+    reference sources on this machine, else the C restatement of it) on a
+    bounded sample of the same workload, all host threads."""
+    if rank != 0:
+        return None
+    import numpy as np
+
+    import oracle
+    from oracle import ref as oref
+
+    n, K, S = 14, 1000, 1024
+    sub = 54  # strings per step (1/16 of 861): bounded sample
+    rng = np.random.default_rng(1002)
+    strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
+    P = len(strings)
+    h = (rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))) * np.sqrt(1.0 / (2 * P))
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    use_ref = oref.available()
+    fn = oref.summed_expectation if use_ref else oracle.summed_expectation
+    for _ in range(args.warmup):
+        fn(strings[:sub], h[:sub], psi)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        fn(strings[:sub], h[:sub], psi)
+    t = (time.perf_counter() - t0) / args.steps
+    terms = sub * (1 << n) * S
+    v = terms / t
+    kind = "reference" if use_ref else "port"
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128/f64", "data": "synthetic",
+            "config": {"workload": "SummedPauliOp.expectation_value float64: n=14, 861 weight<=2 strings, "
+                                   "K=1000, states 16384x1024 complex128",
+                       "sample_per_step": f"{sub} of {P} strings, K=1000, all states"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": oracle.max_threads(), "kind": kind,
+                             "sample": f"{sub} of {P} strings per step"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--profile", action="store_true", help="short device-only run for ncu captures")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-mixed", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        tdist.init_process_group("nccl")
+        dist = tdist
+    try:
+        line = run_ours(args, rank, world, dist)
+        if line is not None and rank == 0:
+            print(json.dumps(line), flush=True)
+    finally:
+        if dist:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

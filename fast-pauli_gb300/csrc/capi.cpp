@@ -6,6 +6,7 @@
 #include "fpg.h"
 
 #include <algorithm>
+#include <atomic>
 #include <initializer_list>
 #include <cstdio>
 #include <cstring>
@@ -23,9 +24,15 @@ using namespace fpg;
 // ---------------------------------------------------------------------------
 
 static thread_local std::string g_last_error;
+static std::atomic<uint64_t> g_launches{0};
 
 namespace fpg
 {
+cudaError_t launched()
+{
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+}
 int set_error(int code, const std::string &msg)
 {
     g_last_error = msg;
@@ -320,6 +327,14 @@ extern "C"
         return g_last_error.c_str();
     }
 
+    int fpg_kernel_launches(uint64_t *total)
+    {
+        if (!total)
+            return set_error(FPG_ERR_INVALID, "total is null");
+        *total = g_launches.load(std::memory_order_relaxed);
+        return FPG_OK;
+    }
+
     int fpg_device_count(int *count)
     {
         if (!count)
@@ -419,6 +434,29 @@ extern "C"
             *n_strings = op->P;
         if (n_groups)
             *n_groups = (int64_t)op->groups.size();
+        return FPG_OK;
+    }
+
+    int fpg_operator_stats(const fpg_operator *op, int64_t *n_chunks, int64_t *row_visits, int64_t *sign_adds)
+    {
+        if (!op)
+            return set_error(FPG_ERR_INVALID, "op is null");
+        const int64_t D = (int64_t)1 << op->n;
+        int64_t visits = 0, adds = 0;
+        for (int c = 0; c < kNumChunkClasses; ++c)
+            for (int i = op->class_begin[(size_t)c]; i < op->class_begin[(size_t)c + 1]; ++i)
+            {
+                const bool paired = (op->chunks[(size_t)i].x >> 5) != 0;
+                const int64_t rows = paired ? D / 2 : D;
+                visits += rows;
+                adds += rows * (kChunkClasses[c].ge + kChunkClasses[c].go);
+            }
+        if (n_chunks)
+            *n_chunks = (int64_t)op->chunks.size();
+        if (row_visits)
+            *row_visits = visits;
+        if (sign_adds)
+            *sign_adds = adds;
         return FPG_OK;
     }
 

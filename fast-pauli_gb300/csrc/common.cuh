@@ -62,9 +62,11 @@ struct DevOp
 };
 
 // ---------------------------------------------------------------------------
-// launchers (implemented in k_*.cu); all enqueue on `st` and return the
-// cudaError_t of the launch.
+// launchers (implemented in k_*.cu); each enqueues one kernel on `st` and
+// returns launched(): the launch's cudaError_t, after counting the launch
+// (fpg_kernel_launches reports the running total).
 // ---------------------------------------------------------------------------
+cudaError_t launched();
 
 // Chunk classes of the expectation kernel: (max even strings, max odd strings).
 constexpr int kNumChunkClasses = 8;

@@ -163,7 +163,7 @@ cudaError_t launch_prep_coeffs(bool fp32, const DevOp &op, const void *coeffs, i
     else
         k_prep_coeffs<double2><<<blocks, 256, 0, st>>>(op.recs, op.orig, op.P, (const double2 *)coeffs, K,
                                                        (double2 *)cw);
-    return cudaGetLastError();
+    return launched();
 }
 
 cudaError_t launch_prep_weighted(bool fp32, const DevOp &op, const void *W, int64_t S, void *cw, cudaStream_t st)
@@ -179,7 +179,7 @@ cudaError_t launch_prep_weighted(bool fp32, const DevOp &op, const void *W, int6
     else
         k_prep_weighted<double2><<<grid, 256, 0, st>>>(op.recs, op.orig, op.P, (const double2 *)W, S,
                                                        (double2 *)cw);
-    return cudaGetLastError();
+    return launched();
 }
 
 cudaError_t launch_apply(bool fp32, bool weighted, const DevOp &op, const void *cw, const void *psi, void *out,
@@ -209,7 +209,7 @@ cudaError_t launch_apply(bool fp32, bool weighted, const DevOp &op, const void *
             k_apply<double, false><<<grid, 256, 0, st>>>((const double *)psi, (double *)out, S, op.n, op.groups,
                                                          op.G, op.recs, (const double2 *)cw, TC);
     }
-    return cudaGetLastError();
+    return launched();
 }
 
 cudaError_t launch_sparse_repr(uint64_t x, uint64_t z, int ny, int n, uint64_t *cols, void *vals, cudaStream_t st)
@@ -219,7 +219,7 @@ cudaError_t launch_sparse_repr(uint64_t x, uint64_t z, int ny, int n, uint64_t *
     if (blocks > 152 * 32)
         blocks = 152 * 32;
     k_sparse_repr<<<(unsigned)blocks, 256, 0, st>>>(x, z, ny, D, cols, (double2 *)vals);
-    return cudaGetLastError();
+    return launched();
 }
 
 } // namespace fpg

@@ -153,7 +153,7 @@ cudaError_t launch_contract_real(bool out_c64, const void *H, bool h_c64, const 
         k_gemm_cr<double2, double, float2, true, true><<<grid, 256, 0, st>>>(H, K, E, K, S, P, (float2 *)out);
     else
         k_gemm_cr<float2, double, double2, true, true><<<grid, 256, 0, st>>>(H, K, E, K, S, P, (double2 *)out);
-    return cudaGetLastError();
+    return launched();
 }
 
 cudaError_t launch_weighted_coeffs(bool fp32, const void *H, const void *X, int64_t P, int64_t K, int64_t S, void *W,
@@ -168,7 +168,7 @@ cudaError_t launch_weighted_coeffs(bool fp32, const void *H, const void *X, int6
     else
         k_gemm_cr<float2, float, float2, false, false>
             <<<grid, 256, 0, st>>>(H, K, (const float *)X, P, S, K, (float2 *)W);
-    return cudaGetLastError();
+    return launched();
 }
 
 } // namespace fpg

@@ -288,7 +288,7 @@ cudaError_t launch_v(const T *psi, int64_t S, int n, const DevOp &op, const Chun
         return cudaErrorInvalidValue;
     }
 #undef FPG_CASE
-    return cudaGetLastError();
+    return launched();
 }
 
 __global__ void k_reduce_splits(const double *__restrict__ partial, int n_splits, int64_t count,
@@ -325,7 +325,7 @@ cudaError_t launch_reduce_splits(const double *partial, int n_splits, int64_t co
     if (blocks > 152 * 16)
         blocks = 152 * 16;
     k_reduce_splits<<<(unsigned)blocks, 256, 0, st>>>(partial, n_splits, count, ev);
-    return cudaGetLastError();
+    return launched();
 }
 
 } // namespace fpg

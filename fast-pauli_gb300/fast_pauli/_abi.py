@@ -37,11 +37,13 @@ _PI64 = ctypes.POINTER(ctypes.c_int64)
 SIGNATURES = {
     "fpg_abi_version": (ctypes.c_int, []),
     "fpg_last_error": (ctypes.c_char_p, []),
+    "fpg_kernel_launches": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint64)]),
     "fpg_device_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int)]),
     "fpg_pointer_is_device": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
     "fpg_operator_create": (ctypes.c_int, [ctypes.c_char_p, _I64, _I32, ctypes.POINTER(_P)]),
     "fpg_operator_destroy": (ctypes.c_int, [_P]),
     "fpg_operator_info": (ctypes.c_int, [_P, _PI32, _PI64, _PI64]),
+    "fpg_operator_stats": (ctypes.c_int, [_P, _PI64, _PI64, _PI64]),
     "fpg_sparse_repr": (ctypes.c_int, [ctypes.c_char_p, _I32, _P, _P, _P]),
     "fpg_apply": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I32, _P]),
     "fpg_expect_strings": (ctypes.c_int, [_P, _P, _P, _I64, _I32, _P]),
@@ -73,6 +75,12 @@ def lib() -> ctypes.CDLL:
     return _lib
 
 
+def kernel_launches() -> int:
+    v = ctypes.c_uint64()
+    check(lib().fpg_kernel_launches(ctypes.byref(v)))
+    return int(v.value)
+
+
 def check(rc: int) -> None:
     if rc != FPG_OK:
         raise FpgError(rc, lib().fpg_last_error().decode())
@@ -99,6 +107,14 @@ class Operator:
         g = ctypes.c_int64()
         check(lib().fpg_operator_info(self._h, ctypes.byref(n), ctypes.byref(p), ctypes.byref(g)))
         return n.value, p.value, g.value
+
+    def stats(self) -> tuple[int, int, int]:
+        """(chunks, row visits per column, signed accumulations per column)."""
+        c = ctypes.c_int64()
+        v = ctypes.c_int64()
+        a = ctypes.c_int64()
+        check(lib().fpg_operator_stats(self._h, ctypes.byref(c), ctypes.byref(v), ctypes.byref(a)))
+        return c.value, v.value, a.value
 
     def close(self) -> None:
         if self._h:

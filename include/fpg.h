@@ -69,6 +69,10 @@ int fpg_abi_version(void);
 /* Message for the calling thread's most recent failure ("" if none). */
 const char *fpg_last_error(void);
 
+/* Running total of kernels this library has launched (all devices, all
+ * threads); lets a caller count the kernels inside a timed region. */
+int fpg_kernel_launches(uint64_t *total);
+
 /* Number of visible CUDA devices (0 on a machine without a GPU). */
 int fpg_device_count(int *count);
 
@@ -86,6 +90,14 @@ int fpg_pointer_is_device(const void *ptr, int *is_device);
 int fpg_operator_create(const char *strings, int64_t n_strings, int32_t n_qubits, fpg_operator **out);
 int fpg_operator_destroy(fpg_operator *op);
 int fpg_operator_info(const fpg_operator *op, int32_t *n_qubits, int64_t *n_strings, int64_t *n_groups);
+
+/*
+ * Work of one expectation pass per state column: number of chunks (CTA work
+ * units), row visits summed over chunks (a visit loads a row pair and forms
+ * conj(psi_i) psi_{i^x}), and signed accumulations (string slots x visits).
+ * Used to report arithmetic rooflines; no counterpart in the reference.
+ */
+int fpg_operator_stats(const fpg_operator *op, int64_t *n_chunks, int64_t *row_visits, int64_t *sign_adds);
 
 /*
  * Sparse pattern of one Pauli string on the device: cols[i] = column of the
