@@ -149,6 +149,28 @@ int fpg_summed_apply(const fpg_operator *op, const void *coeffs, int64_t n_opera
 int fpg_summed_apply_weighted(const fpg_operator *op, const void *coeffs, int64_t n_operators, const void *states,
                               const void *data, void *out, int64_t n_states, int32_t dtype, void *stream);
 
+/*
+ * fpg_summed_expect_noalloc: the same result as fpg_summed_expect
+ * (out(K,S) += sum_j coeffs(j,k) <psi_t|P_j|psi_t>), for callers that cannot
+ * allocate device memory: processes living inside a framework that has
+ * already reserved almost all of the GPU for its own pool (where cudaMalloc
+ * fails or bypasses that pool), and latency-bound request loops that may not
+ * allocate because an allocation can block or synchronise the device.  It
+ * takes the strings themselves (no fpg_operator, whose creation allocates),
+ * allocates nothing, and keeps its scratch -- the encoded strings and the
+ * n_strings x n_states float64 table of per-string expectation values -- in
+ * one 16 MiB static device array that every GPU loading libfpg.so holds until
+ * exit.
+ * Limits: n_strings <= 8192 and n_strings * n_states up to about 2 million
+ * (the table must fit the array); larger requests return FPG_ERR_INVALID.
+ * The first call on a device resolves the array's address (make it before any
+ * stream capture); calls whose GPU work overlaps race on the shared array.
+ * No counterpart in the reference.
+ */
+int fpg_summed_expect_noalloc(const char *strings, int64_t n_strings, int32_t n_qubits, const void *coeffs,
+                              int64_t n_operators, const void *states, void *out, int64_t n_states, int32_t dtype,
+                              void *stream);
+
 #ifdef __cplusplus
 }
 #endif
