@@ -327,6 +327,14 @@ extern "C"
         return g_last_error.c_str();
     }
 
+    int fpg_device_error(int *code, void *stream)
+    {
+        if (!code)
+            return set_error(FPG_ERR_INVALID, "code is null");
+        FPG_CUDA(read_device_error(code, (cudaStream_t)stream));
+        return FPG_OK;
+    }
+
     int fpg_kernel_launches(uint64_t *total)
     {
         if (!total)
@@ -524,6 +532,15 @@ extern "C"
         FPG_CUDA(evb.alloc((size_t)op->P * (size_t)n_states * sizeof(double)));
         if (int rc = run_expect_strings(op, states, (double *)evb.p, n_states, fp32, st))
             return rc;
+        if (fp32)
+        {
+            // mixed path: 3xTF32 contraction on the tensor cores
+            Scratch ws(st);
+            FPG_CUDA(ws.alloc(tc_workspace_bytes(2 * n_operators, n_states, op->P)));
+            FPG_CUDA(launch_contract_tc_expect(coeffs, (const double *)evb.p, op->P, n_operators, n_states, out,
+                                               ws.p, st));
+            return FPG_OK;
+        }
         FPG_CUDA(launch_contract_real(fp32, coeffs, fp32, (const double *)evb.p, op->P, n_operators, n_states, out,
                                       st));
         return FPG_OK;
@@ -613,7 +630,15 @@ extern "C"
         Scratch w(st), cw(st);
         FPG_CUDA(w.alloc((size_t)op->P * (size_t)n_states * csz));
         FPG_CUDA(cw.alloc((size_t)op->P * (size_t)n_states * csz));
-        FPG_CUDA(launch_weighted_coeffs(fp32, coeffs, data, op->P, n_operators, n_states, w.p, st));
+        if (fp32)
+        {
+            // mixed path: weighted coefficients with the 3xTF32 tensor-core GEMM
+            Scratch ws(st);
+            FPG_CUDA(ws.alloc(tc_workspace_bytes(2 * op->P, n_states, n_operators)));
+            FPG_CUDA(launch_weighted_tc(coeffs, (const float *)data, op->P, n_operators, n_states, w.p, ws.p, st));
+        }
+        else
+            FPG_CUDA(launch_weighted_coeffs(fp32, coeffs, data, op->P, n_operators, n_states, w.p, st));
         FPG_CUDA(launch_prep_weighted(fp32, dop, w.p, n_states, cw.p, st));
         FPG_CUDA(launch_apply(fp32, true, dop, cw.p, states, out, n_states, st));
         return FPG_OK;

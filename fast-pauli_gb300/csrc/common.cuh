@@ -96,6 +96,19 @@ cudaError_t launch_reduce_splits(const double *partial, int n_splits, int64_t co
 cudaError_t launch_contract_real(bool out_c64, const void *H, bool h_c64, const double *E, int64_t P, int64_t K,
                                  int64_t S, void *out, cudaStream_t st);
 
+// Tensor-core (tcgen05, 3xTF32, float32 accumulation) forms for the mixed
+// path; ws must hold tc_workspace_bytes(M, N, Kd) of the GEMM they run:
+//   expectation: M = 2K, N = S, Kd = P;   weighted: M = 2P, N = S, Kd = K.
+size_t tc_workspace_bytes(int64_t M, int64_t N, int64_t Kd);
+// out(K,S) complex64 += H^T E with H complex64 (P,K), E float64 (P,S)
+cudaError_t launch_contract_tc_expect(const void *H, const double *E, int64_t P, int64_t K, int64_t S, void *out,
+                                      void *ws, cudaStream_t st);
+// W(P,S) complex64 = H X with H complex64 (P,K), X float32 (K,S)
+cudaError_t launch_weighted_tc(const void *H, const float *X, int64_t P, int64_t K, int64_t S, void *W, void *ws,
+                               cudaStream_t st);
+// Reads and clears the tensor-core kernels' device error flag (synchronises st).
+cudaError_t read_device_error(int *code, cudaStream_t st);
+
 // W(P,S) complex = H(P,K) complex * X(K,S) real.  Overwrites W.  Precision by fp32.
 cudaError_t launch_weighted_coeffs(bool fp32, const void *H, const void *X, int64_t P, int64_t K, int64_t S, void *W,
                                    cudaStream_t st);

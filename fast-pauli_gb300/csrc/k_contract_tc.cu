@@ -1,0 +1,473 @@
+// k_contract_tc.cu -- 3xTF32 coefficient contraction on the 5th-generation
+// tensor cores (tcgen05 + TMEM), for the mixed (complex64) path.
+//
+// Contraction of SummedPauliOp::expectation_value
+// (fast_pauli/cpp/include/__summed_pauli_op.hpp:579-591) and the weighted
+// coefficients of apply_weighted (__summed_pauli_op.hpp:420-432), both as a
+// real GEMM  C(M,N) = A(M,Kd) B(N,Kd)^T  with float32 accumulation:
+//   * expectation: A = [Re H^T; Im H^T] (2K x P), B = E^T (S x P), C (2K x S);
+//   * apply_weighted: A = [Re H; Im H] (2P x K), B = X^T (S x K), C (2P x S).
+// Split precision (3xTF32): every operand x = x_hi + x_lo with
+// x_hi = tf32(x) (round to nearest) and x_lo = tf32(x - x_hi); the product is
+// A_hi B_hi + A_hi B_lo + A_lo B_hi, accumulated in float32 in TMEM.
+//
+// Data movement: a prep kernel writes each operand in the canonical K-major,
+// no-swizzle core-matrix layout (8 rows x 16 bytes per core matrix), one
+// contiguous 16 KiB block per (128-row tile, 32-deep k chunk), so the GEMM
+// moves blocks with 1-D TMA bulk copies (cp.async.bulk, completion on an
+// mbarrier).  One elected thread issues copies and tcgen05.mma (M=128,
+// N=128, K=8 per instruction, 3 per k step); tcgen05.commit signals stage
+// reuse; a two-stage ring overlaps copies with MMAs.  The epilogue reads the
+// 128x128 float32 accumulator with tcgen05.ld (warp w owns TMEM lanes
+// 32w..32w+31) and writes a row-major float32 tile.
+//
+// Every mbarrier wait is bounded; on timeout the kernel records an error code
+// (fpg_device_error reports it), still waits (bounded) for its own copies and
+// MMAs, frees its TMEM and returns.
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace fpg
+{
+
+__device__ int g_tc_error = 0;
+
+namespace
+{
+
+constexpr int TM = 128, TN = 128, TK = 32;           // CTA tile and k chunk (tf32 elements)
+constexpr int BLOCK_BYTES = TM * TK * 4;             // 16 KiB per operand block
+constexpr int STAGE_BYTES = 4 * BLOCK_BYTES;         // A_hi, A_lo, B_hi, B_lo
+constexpr int NSTAGE = 2;
+constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024; // + barriers / TMEM address (alignment slack)
+constexpr uint32_t TMEM_COLS = 128;
+constexpr long long WAIT_LIMIT = 1ll << 22;          // mbarrier polls before giving up
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// bounded wait on phase `parity`; returns false on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    const uint32_t a = smem_u32(bar);
+    for (long long it = 0; it < WAIT_LIMIT; ++it)
+    {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done)
+                     : "r"(a), "r"(parity)
+                     : "memory");
+        if (done)
+            return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Shared-memory matrix descriptor: start >> 4 (bits 0-13), leading byte
+// offset >> 4 (16-29; K-direction stride between core matrices), stride byte
+// offset >> 4 (32-45; stride between 8-row groups), descriptor version 1
+// (bits 46-47), no swizzle (bits 61-63 = 0).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor, kind::tf32: D = f32 (bits 4-5 = 1), A = B = tf32
+// (bits 7-9 and 10-12 = 2), both K-major, N >> 3 at bits 17-22, M >> 4 at
+// bits 24-28.
+constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t accumulate)
+{
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "setp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+                 "l"(da), "l"(db), "r"(IDESC), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ float tf32_rna(float x)
+{
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+// byte offset of element (row r, k) inside a 128 x 32 operand block
+__device__ __forceinline__ uint32_t block_offset(int r, int k)
+{
+    return (uint32_t)((r >> 3) * 1024 + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4);
+}
+
+// --------------------------------------------------------------- operand prep
+// Writes hi/lo tf32 blocks for a rows x depth operand whose element (r, k) is
+// produced by `load(r, k)` (zero outside the logical size).  Block index =
+// row_tile * n_kchunks + kchunk.
+template <typename Load>
+__device__ void write_operand(Load load, int64_t rows, int64_t depth, int64_t rows_pad, int64_t depth_pad,
+                              float *hi, float *lo)
+{
+    const int64_t kchunks = depth_pad / TK;
+    const int64_t total = rows_pad * depth_pad;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int64_t r = e / depth_pad, k = e - r * depth_pad;
+        double v = (r < rows && k < depth) ? load(r, k) : 0.0;
+        const float f = (float)v;
+        const float h = tf32_rna(f);
+        const float l = tf32_rna((float)(v - (double)h));
+        const int64_t blk = (r / TM) * kchunks + (k / TK);
+        const int64_t off = blk * (BLOCK_BYTES / 4) + block_offset((int)(r % TM), (int)(k % TK)) / 4;
+        hi[off] = h;
+        lo[off] = l;
+    }
+}
+
+// expectation: A(m, p) = m < K ? Re H[p][m] : Im H[p][m-K];  H complex64 (P,K)
+__global__ void k_prep_a_expect(const float2 *__restrict__ H, int64_t P, int64_t K, int64_t rows_pad,
+                                int64_t depth_pad, float *hi, float *lo)
+{
+    write_operand(
+        [&](int64_t m, int64_t p) -> double {
+            const float2 h = H[p * K + (m < K ? m : m - K)];
+            return m < K ? h.x : h.y;
+        },
+        2 * K, P, rows_pad, depth_pad, hi, lo);
+}
+
+// expectation: B(t, p) = E[p][t];  E float64 (P,S)
+__global__ void k_prep_b_expect(const double *__restrict__ E, int64_t P, int64_t S, int64_t rows_pad,
+                                int64_t depth_pad, float *hi, float *lo)
+{
+    write_operand([&](int64_t t, int64_t p) -> double { return E[p * S + t]; }, S, P, rows_pad, depth_pad, hi, lo);
+}
+
+// weighted: A(m, k) = m < P ? Re H[m][k] : Im H[m-P][k]
+__global__ void k_prep_a_weighted(const float2 *__restrict__ H, int64_t P, int64_t K, int64_t rows_pad,
+                                  int64_t depth_pad, float *hi, float *lo)
+{
+    write_operand(
+        [&](int64_t m, int64_t k) -> double {
+            const float2 h = H[(m < P ? m : m - P) * K + k];
+            return m < P ? h.x : h.y;
+        },
+        2 * P, K, rows_pad, depth_pad, hi, lo);
+}
+
+// weighted: B(t, k) = X[k][t];  X float32 (K,S)
+__global__ void k_prep_b_weighted(const float *__restrict__ X, int64_t K, int64_t S, int64_t rows_pad,
+                                  int64_t depth_pad, float *hi, float *lo)
+{
+    write_operand([&](int64_t t, int64_t k) -> double { return X[k * S + t]; }, S, K, rows_pad, depth_pad, hi,
+                  lo);
+}
+
+// ------------------------------------------------------------------- GEMM
+// C (rows_pad x cols_pad, row-major float32) = A B^T for one 128x128 tile per CTA.
+__global__ void __launch_bounds__(128, 1)
+    k_gemm_tf32x3(const float *__restrict__ a_hi, const float *__restrict__ a_lo, const float *__restrict__ b_hi,
+                  const float *__restrict__ b_lo, int64_t kchunks, int64_t cols_pad, float *__restrict__ C)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // 1024-byte aligned ring of stages, then barriers
+    unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *full = (uint64_t *)(smem + NSTAGE * STAGE_BYTES);
+    uint64_t *empty = full + NSTAGE;
+    uint64_t *done = empty + NSTAGE;
+    uint32_t *tmem_slot = (uint32_t *)(done + 1);
+    int *status = (int *)(tmem_slot + 1); // producer's verdict, shared with the epilogue
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t mt = blockIdx.y, nt = blockIdx.x;
+
+    if (threadIdx.x == 0)
+    {
+        for (int s = 0; s < NSTAGE; ++s)
+        {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        *status = 1;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    bool ok = true;
+    if (threadIdx.x == 0)
+    {
+        const float *srcs[4];
+        auto issue = [&](int64_t kc, int s) {
+            srcs[0] = a_hi + (mt * kchunks + kc) * (BLOCK_BYTES / 4);
+            srcs[1] = a_lo + (mt * kchunks + kc) * (BLOCK_BYTES / 4);
+            srcs[2] = b_hi + (nt * kchunks + kc) * (BLOCK_BYTES / 4);
+            srcs[3] = b_lo + (nt * kchunks + kc) * (BLOCK_BYTES / 4);
+            mbar_expect_tx(&full[s], STAGE_BYTES);
+            for (int q = 0; q < 4; ++q)
+                bulk_copy_g2s(smem + s * STAGE_BYTES + q * BLOCK_BYTES, srcs[q], BLOCK_BYTES, &full[s]);
+        };
+        uint32_t full_phase[NSTAGE] = {0, 0}, empty_phase[NSTAGE] = {0, 0};
+        int64_t issued = 0;
+        for (; issued < kchunks && issued < NSTAGE; ++issued)
+            issue(issued, (int)issued);
+        int64_t committed = 0;
+        for (int64_t kc = 0; kc < kchunks && ok; ++kc)
+        {
+            const int s = (int)(kc % NSTAGE);
+            if (!mbar_wait(&full[s], full_phase[s]))
+            {
+                ok = false;
+                break;
+            }
+            full_phase[s] ^= 1u;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t base = smem_u32(smem + s * STAGE_BYTES);
+            for (int ks = 0; ks < TK / 8; ++ks)
+            {
+                // one k step = 8 tf32 = two 16-byte core-matrix columns
+                const uint32_t koff = (uint32_t)ks * 256u;
+                const uint64_t dah = smem_desc(base + 0 * BLOCK_BYTES + koff, 128, 1024);
+                const uint64_t dal = smem_desc(base + 1 * BLOCK_BYTES + koff, 128, 1024);
+                const uint64_t dbh = smem_desc(base + 2 * BLOCK_BYTES + koff, 128, 1024);
+                const uint64_t dbl = smem_desc(base + 3 * BLOCK_BYTES + koff, 128, 1024);
+                const uint32_t acc0 = (kc > 0 || ks > 0) ? 1u : 0u;
+                mma_tf32(tmem, dah, dbh, acc0);
+                mma_tf32(tmem, dah, dbl, 1u);
+                mma_tf32(tmem, dal, dbh, 1u);
+            }
+            mma_commit(&empty[s]);
+            committed = kc + 1;
+            if (issued < kchunks)
+            {
+                // stage s is refilled once the MMAs that read it have completed
+                if (!mbar_wait(&empty[s], empty_phase[s]))
+                {
+                    ok = false;
+                    break;
+                }
+                empty_phase[s] ^= 1u;
+                issue(issued, s);
+                ++issued;
+            }
+        }
+        // all MMAs issued so far complete before `done` arrives
+        mma_commit(done);
+        if (!ok)
+        {
+            atomicExch(&g_tc_error, 1);
+            // drain our own copies still in flight (bounded)
+            for (int s = 0; s < NSTAGE; ++s)
+                (void)mbar_wait(&full[s], full_phase[s]);
+        }
+        (void)committed;
+        *status = ok ? 1 : 0;
+    }
+    __syncthreads();
+    ok = *status != 0;
+    const bool done_ok = mbar_wait(done, 0);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+    if (done_ok && ok)
+    {
+        // epilogue: warp w reads TMEM lanes 32w..32w+31 = tile rows, 32 columns per load
+        const int64_t row = mt * TM + warp * 32 + lane;
+        for (int c0 = 0; c0 < TN; c0 += 32)
+        {
+            uint32_t r[32];
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                         "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                         "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                           "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                           "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+                           "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+                           "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                         : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            float *dst = C + row * cols_pad + nt * TN + c0;
+#pragma unroll
+            for (int j = 0; j < 32; j += 4)
+                *reinterpret_cast<float4 *>(dst + j) = make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]),
+                                                                   __uint_as_float(r[j + 2]),
+                                                                   __uint_as_float(r[j + 3]));
+        }
+    }
+    else if (threadIdx.x == 0)
+    {
+        atomicExch(&g_tc_error, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS)
+                     : "memory");
+}
+
+// -------------------------------------------------------------- epilogues
+// expectation: out[k][t] += (C[k][t], C[K+k][t])   (complex64 out)
+__global__ void k_finish_expect(const float *__restrict__ C, int64_t cols_pad, int64_t K, int64_t S,
+                                float2 *__restrict__ out)
+{
+    const int64_t total = K * S;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int64_t k = e / S, t = e - k * S;
+        float2 o = out[e];
+        o.x += C[k * cols_pad + t];
+        o.y += C[(K + k) * cols_pad + t];
+        out[e] = o;
+    }
+}
+
+// weighted: W[p][t] = (C[p][t], C[P+p][t])
+__global__ void k_finish_weighted(const float *__restrict__ C, int64_t cols_pad, int64_t P, int64_t S,
+                                  float2 *__restrict__ W)
+{
+    const int64_t total = P * S;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int64_t p = e / S, t = e - p * S;
+        W[e] = make_float2(C[p * cols_pad + t], C[(P + p) * cols_pad + t]);
+    }
+}
+
+int64_t round_up(int64_t v, int64_t m)
+{
+    return (v + m - 1) / m * m;
+}
+
+unsigned grid_for(int64_t n)
+{
+    int64_t b = (n + 255) / 256;
+    return (unsigned)(b < 1 ? 1 : (b > 152 * 16 ? 152 * 16 : b));
+}
+
+} // namespace
+
+size_t tc_workspace_bytes(int64_t M, int64_t N, int64_t Kd)
+{
+    const int64_t Mp = round_up(M, TM), Np = round_up(N, TN), Kp = round_up(Kd, TK);
+    return (size_t)(2 * Mp * Kp + 2 * Np * Kp + Mp * Np) * sizeof(float) + 256;
+}
+
+static cudaError_t run_gemm(int64_t M, int64_t N, int64_t Kd, void *ws, float **a_hi, float **a_lo, float **b_hi,
+                            float **b_lo, float **C, int64_t *Mp_out, int64_t *Np_out, int64_t *Kp_out)
+{
+    const int64_t Mp = round_up(M, TM), Np = round_up(N, TN), Kp = round_up(Kd, TK);
+    float *p = (float *)(((uintptr_t)ws + 255) & ~(uintptr_t)255);
+    *a_hi = p;
+    *a_lo = *a_hi + Mp * Kp;
+    *b_hi = *a_lo + Mp * Kp;
+    *b_lo = *b_hi + Np * Kp;
+    *C = *b_lo + Np * Kp;
+    *Mp_out = Mp;
+    *Np_out = Np;
+    *Kp_out = Kp;
+    return cudaSuccess;
+}
+
+cudaError_t launch_contract_tc_expect(const void *H, const double *E, int64_t P, int64_t K, int64_t S, void *out,
+                                      void *ws, cudaStream_t st)
+{
+    if (K <= 0 || S <= 0 || P <= 0)
+        return cudaSuccess;
+    float *ah, *al, *bh, *bl, *C;
+    int64_t Mp, Np, Kp;
+    run_gemm(2 * K, S, P, ws, &ah, &al, &bh, &bl, &C, &Mp, &Np, &Kp);
+    cudaError_t e;
+    k_prep_a_expect<<<grid_for(Mp * Kp), 256, 0, st>>>((const float2 *)H, P, K, Mp, Kp, ah, al);
+    if ((e = launched()))
+        return e;
+    k_prep_b_expect<<<grid_for(Np * Kp), 256, 0, st>>>(E, P, S, Np, Kp, bh, bl);
+    if ((e = launched()))
+        return e;
+    if ((e = cudaFuncSetAttribute(k_gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES)))
+        return e;
+    dim3 grid((unsigned)(Np / TN), (unsigned)(Mp / TM));
+    k_gemm_tf32x3<<<grid, 128, SMEM_BYTES, st>>>(ah, al, bh, bl, Kp / TK, Np, C);
+    if ((e = launched()))
+        return e;
+    k_finish_expect<<<grid_for(K * S), 256, 0, st>>>(C, Np, K, S, (float2 *)out);
+    return launched();
+}
+
+cudaError_t launch_weighted_tc(const void *H, const float *X, int64_t P, int64_t K, int64_t S, void *W, void *ws,
+                               cudaStream_t st)
+{
+    if (P <= 0 || S <= 0)
+        return cudaSuccess;
+    float *ah, *al, *bh, *bl, *C;
+    int64_t Mp, Np, Kp;
+    run_gemm(2 * P, S, K, ws, &ah, &al, &bh, &bl, &C, &Mp, &Np, &Kp);
+    cudaError_t e;
+    k_prep_a_weighted<<<grid_for(Mp * Kp), 256, 0, st>>>((const float2 *)H, P, K, Mp, Kp, ah, al);
+    if ((e = launched()))
+        return e;
+    k_prep_b_weighted<<<grid_for(Np * Kp), 256, 0, st>>>(X, K, S, Np, Kp, bh, bl);
+    if ((e = launched()))
+        return e;
+    if ((e = cudaFuncSetAttribute(k_gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES)))
+        return e;
+    dim3 grid((unsigned)(Np / TN), (unsigned)(Mp / TM));
+    k_gemm_tf32x3<<<grid, 128, SMEM_BYTES, st>>>(ah, al, bh, bl, Kp / TK, Np, C);
+    if ((e = launched()))
+        return e;
+    k_finish_weighted<<<grid_for(P * S), 256, 0, st>>>(C, Np, P, S, (float2 *)W);
+    return launched();
+}
+
+cudaError_t read_device_error(int *code, cudaStream_t st)
+{
+    int v = 0;
+    cudaError_t e = cudaMemcpyFromSymbolAsync(&v, g_tc_error, sizeof(int), 0, cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess)
+        return e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return e;
+    *code = v;
+    const int zero = 0;
+    return cudaMemcpyToSymbolAsync(g_tc_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, st);
+}
+
+} // namespace fpg

@@ -38,6 +38,7 @@ SIGNATURES = {
     "fpg_abi_version": (ctypes.c_int, []),
     "fpg_last_error": (ctypes.c_char_p, []),
     "fpg_kernel_launches": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint64)]),
+    "fpg_device_error": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), _P]),
     "fpg_device_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int)]),
     "fpg_pointer_is_device": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
     "fpg_operator_create": (ctypes.c_int, [ctypes.c_char_p, _I64, _I32, ctypes.POINTER(_P)]),

@@ -73,6 +73,12 @@ const char *fpg_last_error(void);
  * threads); lets a caller count the kernels inside a timed region. */
 int fpg_kernel_launches(uint64_t *total);
 
+/* Status of the library's bounded device waits since the last call: *code = 0
+ * if every wait completed, FPG_ERR_TIMEOUT-class failure (nonzero) if a
+ * tensor-core kernel gave up waiting on an mbarrier (its results are then
+ * invalid).  Synchronises `stream` and clears the flag. */
+int fpg_device_error(int *code, void *stream);
+
 /* Number of visible CUDA devices (0 on a machine without a GPU). */
 int fpg_device_count(int *count);
 

@@ -201,6 +201,57 @@ def test_torch_device_tensors_c128_and_mixed():
     assert normwise(sop.apply(t64).cpu().numpy(), wa) < TOL_MIXED
 
 
+# ------------------------------------------------- tensor-core contraction
+
+
+@pytest.mark.parametrize("K,S,n", [(1, 1, 3), (300, 200, 7), (130, 129, 6)])
+def test_tensor_core_contraction_3xtf32(K, S, n):
+    """Mixed path: the tcgen05 3xTF32 contraction across several 128x128
+    tiles and 32-deep k chunks, isolated from the expectation stage by
+    contracting the same float64 per-string table on the host."""
+    torch = pytest.importorskip("torch")
+    from fast_pauli import _abi
+
+    L = _abi.lib()
+    rng = np.random.default_rng(K + S + n)
+    strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
+    P = len(strings)
+    h = (rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))) / np.sqrt(2 * P)
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    op = _abi.Operator(strings)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    d64 = torch.from_numpy(psi).to(torch.complex64).cuda()
+    h64 = torch.from_numpy(h).to(torch.complex64).cuda()
+    ev = torch.empty((P, S), dtype=torch.float64, device="cuda")
+    _abi.check(L.fpg_expect_strings(op.handle, d64.data_ptr(), ev.data_ptr(), S, _abi.FPG_C64, st))
+    out = torch.zeros((K, S), dtype=torch.complex64, device="cuda")
+    _abi.check(L.fpg_summed_expect(op.handle, h64.data_ptr(), K, d64.data_ptr(), out.data_ptr(), S, _abi.FPG_C64,
+                                   st))
+    code = ctypes.c_int(-1)
+    _abi.check(L.fpg_device_error(ctypes.byref(code), st))
+    assert code.value == 0
+    want = h64.cpu().numpy().astype(np.complex128).T @ ev.cpu().numpy()
+    assert normwise(out.cpu().numpy(), want) < 2e-6  # 3xTF32 with float32 accumulation
+    assert normwise(out.cpu().numpy(), oracle.summed_expectation(strings, h, psi)) < TOL_MIXED
+    op.close()
+
+
+def test_tensor_core_weighted_coefficients():
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(77)
+    n, S, K = 6, 150, 140
+    strings = oracle.uniform_strings(rng, n, 40)
+    P = len(strings)
+    h = rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    data = rng.standard_normal((K, S))
+    sop = fp.SummedPauliOp(strings, h)
+    got = sop.apply_weighted(torch.from_numpy(psi).to(torch.complex64).cuda(),
+                             torch.from_numpy(data).to(torch.float32).cuda())
+    want = oracle.summed_apply_weighted(strings, h, psi, data)
+    assert normwise(got.cpu().numpy(), want) < TOL_MIXED
+
+
 # ------------------------------------------------------------ raw C ABI
 
 
