@@ -1,0 +1,609 @@
+// batch.cu -- many expectation problems of uneven size in one persistent,
+// graph-capturable launch sequence, with a project-written autotuner.
+//
+// A batch holds problems (operator, coefficients (P,K), states (2^n,S),
+// output (K,S)) of different qubit counts, string counts and state counts --
+// e.g. 256 PauliOp.expectation_value calls (reference __pauli_op.hpp:482-549)
+// that would otherwise be 256 separate calls.  Planning turns every problem
+// into work items (entry, chunk, column tile, row split) of the expectation
+// kernel; one persistent kernel per chunk class (at most 8, usually 1-3)
+// pulls items from a device work queue (atomic counter), so small problems
+// fill the gaps left by large ones and no launch is wasted on a tail.  Item
+// order: problems largest first, then column tile, row split, chunk (chunks
+// fastest, so concurrently running CTAs share rows in L2).  Partial sums go
+// to per-problem (split, string, state) tables, reduced in place in a fixed
+// order, then one batched kernel contracts them with the coefficients in
+// float64 and OVERWRITES the outputs.  Every summation order is fixed, so a
+// problem's result does not depend on what else is in the batch or on how
+// the work queue was drained.
+//
+// fpg_batch_run enqueues: counter reset (memset), the persistent kernels, the
+// reduction and the contraction -- no allocation, so the sequence can be
+// captured into a CUDA graph (fpg_batch_run_graph captures once and replays).
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fpg.h"
+
+#include "expect_body.cuh"
+#include "host_internal.hpp"
+
+namespace fpg
+{
+
+struct BatchEntry
+{
+    const void *psi;
+    double *partial; // (n_splits, P, S)
+    const StringRec *recs;
+    const int32_t *orig;
+    const Chunk *chunks;
+    const void *coeffs; // (P, K) complex
+    void *out;          // (K, S) complex
+    int64_t S;
+    int64_t P;
+    int64_t K;
+    int64_t red_off; // offset in the flattened (P*S) index space of the reduction
+    int64_t con_off; // offset in the flattened (K*S) index space of the contraction
+    int32_t n;
+    int32_t TC;
+    int32_t n_splits;
+    int32_t pad;
+};
+
+struct BatchItem
+{
+    int32_t entry;
+    int32_t chunk;
+    int32_t ctile;
+    int32_t split;
+};
+
+namespace
+{
+
+template <typename T, int GE, int GO>
+__global__ void __launch_bounds__(256) k_batch_expect(const BatchEntry *__restrict__ entries,
+                                                      const BatchItem *__restrict__ items, int n_items,
+                                                      int *__restrict__ counter)
+{
+    extern __shared__ double red[]; // blockDim.x doubles
+    __shared__ int s_item;
+    for (;;)
+    {
+        if (threadIdx.x == 0)
+            s_item = atomicAdd(counter, 1);
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it >= n_items)
+            break;
+        const BatchItem bi = items[it];
+        const BatchEntry &e = entries[bi.entry];
+        expect_chunk_body<T, 1, GE, GO>((const T *)e.psi, e.S, e.n, e.recs, e.orig, e.P, e.chunks[bi.chunk], e.TC,
+                                        (int64_t)bi.ctile, bi.split, e.n_splits, e.partial, red);
+    }
+}
+
+__device__ __forceinline__ int find_entry(const BatchEntry *entries, int n_entries, int64_t idx, bool contraction)
+{
+    int lo = 0, hi = n_entries - 1;
+    while (lo < hi)
+    {
+        const int mid = (lo + hi + 1) >> 1;
+        const int64_t off = contraction ? entries[mid].con_off : entries[mid].red_off;
+        if (off <= idx)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// partial[0] = sum over splits, per problem, in split order
+__global__ void k_batch_reduce(const BatchEntry *__restrict__ entries, int n_entries, int64_t total)
+{
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x)
+    {
+        const BatchEntry &e = entries[find_entry(entries, n_entries, g, false)];
+        if (e.n_splits <= 1)
+            continue;
+        const int64_t i = g - e.red_off, cnt = e.P * e.S;
+        double s = e.partial[i];
+        for (int p = 1; p < e.n_splits; ++p)
+            s += e.partial[(int64_t)p * cnt + i];
+        e.partial[i] = s;
+    }
+}
+
+// out(k,t) = sum_j coeffs(j,k) ev(j,t)
+template <typename CT>
+__global__ void k_batch_contract(const BatchEntry *__restrict__ entries, int n_entries, int64_t total)
+{
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x)
+    {
+        const BatchEntry &e = entries[find_entry(entries, n_entries, g, true)];
+        const int64_t i = g - e.con_off;
+        const int64_t k = i / e.S, t = i - k * e.S;
+        const CT *h = (const CT *)e.coeffs;
+        double re = 0.0, im = 0.0;
+        for (int64_t j = 0; j < e.P; ++j)
+        {
+            const CT c = h[j * e.K + k];
+            const double v = e.partial[j * e.S + t];
+            re = fma((double)c.x, v, re);
+            im = fma((double)c.y, v, im);
+        }
+        CT o;
+        o.x = re;
+        o.y = im;
+        ((CT *)e.out)[k * e.S + t] = o;
+    }
+}
+
+} // namespace
+} // namespace fpg
+
+using namespace fpg;
+
+struct fpg_batch
+{
+    int32_t dtype = FPG_C64;
+    int device = 0;
+    struct Problem
+    {
+        const fpg_operator *op;
+        const void *coeffs;
+        int64_t K;
+        const void *psi;
+        void *out;
+        int64_t S;
+    };
+    std::vector<Problem> problems;
+    fpg_batch_tuning tuning{256, 4, 1 << 12};
+    bool planned = false;
+    // device state of the plan
+    BatchEntry *d_entries = nullptr;
+    BatchItem *d_items = nullptr;
+    int *d_counters = nullptr;
+    double *d_partial = nullptr;
+    int class_begin[kNumChunkClasses + 1] = {};
+    int64_t red_total = 0, con_total = 0;
+    int grid = 0;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph = nullptr;
+
+    void free_plan()
+    {
+        if (exec)
+            cudaGraphExecDestroy(exec);
+        if (graph)
+            cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+        cudaFree(d_entries);
+        cudaFree(d_items);
+        cudaFree(d_counters);
+        cudaFree(d_partial);
+        d_entries = nullptr;
+        d_items = nullptr;
+        d_counters = nullptr;
+        d_partial = nullptr;
+        planned = false;
+    }
+};
+
+namespace
+{
+
+int tc_for(int64_t S)
+{
+    int tc = 1;
+    while (tc < 32 && tc < S)
+        tc <<= 1;
+    return tc;
+}
+
+template <typename T>
+cudaError_t launch_class(int cls, int grid, int threads, const BatchEntry *e, const BatchItem *items, int n_items,
+                         int *counter, cudaStream_t st)
+{
+    const size_t smem = (size_t)threads * sizeof(double);
+#define FPG_BCASE(ID, GE, GO)                                                                                          \
+    case ID:                                                                                                           \
+        k_batch_expect<T, GE, GO><<<grid, threads, smem, st>>>(e, items, n_items, counter);                           \
+        break;
+    switch (cls)
+    {
+        FPG_BCASE(0, 1, 0)
+        FPG_BCASE(1, 0, 1)
+        FPG_BCASE(2, 1, 1)
+        FPG_BCASE(3, 2, 2)
+        FPG_BCASE(4, 4, 4)
+        FPG_BCASE(5, 8, 8)
+        FPG_BCASE(6, 8, 0)
+        FPG_BCASE(7, 0, 8)
+    default:
+        return cudaErrorInvalidValue;
+    }
+#undef FPG_BCASE
+    return launched();
+}
+
+int max_resident(int cls, bool fp32, int threads)
+{
+    int nb = 0;
+    const size_t smem = (size_t)threads * sizeof(double);
+    cudaError_t e = cudaSuccess;
+#define FPG_OCC(ID, GE, GO)                                                                                            \
+    case ID:                                                                                                           \
+        e = fp32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_expect<float, GE, GO>, threads, smem)    \
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_expect<double, GE, GO>, threads, smem);  \
+        break;
+    switch (cls)
+    {
+        FPG_OCC(0, 1, 0)
+        FPG_OCC(1, 0, 1)
+        FPG_OCC(2, 1, 1)
+        FPG_OCC(3, 2, 2)
+        FPG_OCC(4, 4, 4)
+        FPG_OCC(5, 8, 8)
+        FPG_OCC(6, 8, 0)
+        FPG_OCC(7, 0, 8)
+    default:
+        break;
+    }
+#undef FPG_OCC
+    if (e != cudaSuccess)
+    {
+        cudaGetLastError();
+        return 1;
+    }
+    return nb < 1 ? 1 : nb;
+}
+
+int do_plan(fpg_batch *b, const fpg_batch_tuning &t)
+{
+    if (t.threads_per_cta != 128 && t.threads_per_cta != 256)
+        return set_error(FPG_ERR_INVALID, "threads_per_cta must be 128 or 256");
+    if (t.ctas_per_sm < 1 || t.ctas_per_sm > 8)
+        return set_error(FPG_ERR_INVALID, "ctas_per_sm must be in [1, 8]");
+    if (t.rows_per_item < 32 || (t.rows_per_item & (t.rows_per_item - 1)))
+        return set_error(FPG_ERR_INVALID, "rows_per_item must be a power of two >= 32");
+    b->free_plan();
+    const int np = (int)b->problems.size();
+    // largest problems first
+    std::vector<int> order((size_t)np);
+    for (int i = 0; i < np; ++i)
+        order[(size_t)i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+        const auto &pa = b->problems[(size_t)a], &pc = b->problems[(size_t)c];
+        const double wa = (double)pa.op->P * (double)(1ll << pa.op->n) * (double)pa.S;
+        const double wc = (double)pc.op->P * (double)(1ll << pc.op->n) * (double)pc.S;
+        return wa > wc;
+    });
+    std::vector<BatchEntry> entries((size_t)np);
+    std::vector<std::vector<BatchItem>> by_class(kNumChunkClasses);
+    int64_t partial_total = 0, red_off = 0, con_off = 0;
+    for (int pos = 0; pos < np; ++pos)
+    {
+        const int i = order[(size_t)pos];
+        const auto &p = b->problems[(size_t)i];
+        const fpg_operator *op = p.op;
+        BatchEntry &e = entries[(size_t)i];
+        e.psi = p.psi;
+        e.recs = op->d_recs;
+        e.orig = op->d_orig;
+        e.chunks = op->d_chunks;
+        e.coeffs = p.coeffs;
+        e.out = p.out;
+        e.S = p.S;
+        e.P = op->P;
+        e.K = p.K;
+        e.n = op->n;
+        e.TC = std::min(tc_for(p.S), t.threads_per_cta);
+        const int64_t NB = op->n >= 5 ? ((int64_t)1 << (op->n - 5)) : 1;
+        const int64_t blocks_per_item = std::max<int64_t>(1, t.rows_per_item / 32);
+        e.n_splits = (int32_t)std::max<int64_t>(1, std::min<int64_t>(64, NB / blocks_per_item));
+        e.red_off = red_off;
+        e.con_off = con_off;
+        red_off += e.P * e.S;
+        con_off += e.K * e.S;
+        partial_total += (int64_t)e.n_splits * e.P * e.S;
+        const int64_t ctiles = (e.S + e.TC - 1) / e.TC;
+        for (int c = 0; c < kNumChunkClasses; ++c)
+            for (int64_t ct = 0; ct < ctiles; ++ct)
+                for (int s = 0; s < e.n_splits; ++s)
+                    for (int ch = op->class_begin[(size_t)c]; ch < op->class_begin[(size_t)c + 1]; ++ch)
+                        by_class[(size_t)c].push_back(BatchItem{i, ch, (int32_t)ct, s});
+    }
+    std::vector<BatchItem> items;
+    for (int c = 0; c < kNumChunkClasses; ++c)
+    {
+        b->class_begin[c] = (int)items.size();
+        items.insert(items.end(), by_class[(size_t)c].begin(), by_class[(size_t)c].end());
+    }
+    b->class_begin[kNumChunkClasses] = (int)items.size();
+    if (items.size() > (size_t)0x7fffffff)
+        return set_error(FPG_ERR_UNSUPPORTED, "batch has too many work items");
+    // device-side partial tables
+    cudaError_t err = cudaSuccess;
+    if ((err = cudaMalloc((void **)&b->d_partial, (size_t)std::max<int64_t>(1, partial_total) * sizeof(double))))
+    {
+        b->free_plan();
+        return cuda_error(err, "fpg_batch_plan: partial tables");
+    }
+    int64_t off = 0;
+    // entries keep the order of addition; offsets into the partial buffer by addition order
+    for (int i = 0; i < np; ++i)
+    {
+        entries[(size_t)i].partial = b->d_partial + off;
+        off += (int64_t)entries[(size_t)i].n_splits * entries[(size_t)i].P * entries[(size_t)i].S;
+    }
+    // red/con offsets must be monotone in entry index for the binary search:
+    // recompute them in addition order
+    red_off = con_off = 0;
+    for (int i = 0; i < np; ++i)
+    {
+        entries[(size_t)i].red_off = red_off;
+        entries[(size_t)i].con_off = con_off;
+        red_off += entries[(size_t)i].P * entries[(size_t)i].S;
+        con_off += entries[(size_t)i].K * entries[(size_t)i].S;
+    }
+    b->red_total = red_off;
+    b->con_total = con_off;
+    if ((err = cudaMalloc((void **)&b->d_entries, entries.size() * sizeof(BatchEntry))) ||
+        (err = cudaMemcpy(b->d_entries, entries.data(), entries.size() * sizeof(BatchEntry),
+                          cudaMemcpyHostToDevice)) ||
+        (err = cudaMalloc((void **)&b->d_items, std::max<size_t>(1, items.size()) * sizeof(BatchItem))) ||
+        (!items.empty() &&
+         (err = cudaMemcpy(b->d_items, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice))) ||
+        (err = cudaMalloc((void **)&b->d_counters, kNumChunkClasses * sizeof(int))))
+    {
+        b->free_plan();
+        return cuda_error(err, "fpg_batch_plan: work queue");
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+    b->grid = sms * t.ctas_per_sm;
+    b->tuning = t;
+    b->planned = true;
+    return FPG_OK;
+}
+
+int do_run(fpg_batch *b, cudaStream_t st)
+{
+    const bool fp32 = b->dtype == FPG_C64;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(b->d_counters, 0, kNumChunkClasses * sizeof(int), st)))
+        return cuda_error(e, "cudaMemsetAsync");
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+    for (int c = 0; c < kNumChunkClasses; ++c)
+    {
+        const int n_items = b->class_begin[c + 1] - b->class_begin[c];
+        if (n_items <= 0)
+            continue;
+        const int cap = sms * max_resident(c, fp32, b->tuning.threads_per_cta);
+        const int grid = std::max(1, std::min({b->grid, cap, n_items}));
+        e = fp32 ? launch_class<float>(c, grid, b->tuning.threads_per_cta, b->d_entries,
+                                       b->d_items + b->class_begin[c], n_items, b->d_counters + c, st)
+                 : launch_class<double>(c, grid, b->tuning.threads_per_cta, b->d_entries,
+                                        b->d_items + b->class_begin[c], n_items, b->d_counters + c, st);
+        if (e)
+            return cuda_error(e, "persistent batch kernel");
+    }
+    const int np = (int)b->problems.size();
+    const unsigned g1 = (unsigned)std::max<int64_t>(1, std::min<int64_t>((b->red_total + 255) / 256, sms * 16));
+    k_batch_reduce<<<g1, 256, 0, st>>>(b->d_entries, np, b->red_total);
+    if ((e = launched()))
+        return cuda_error(e, "batch reduction");
+    const unsigned g2 = (unsigned)std::max<int64_t>(1, std::min<int64_t>((b->con_total + 255) / 256, sms * 16));
+    if (fp32)
+        k_batch_contract<float2><<<g2, 256, 0, st>>>(b->d_entries, np, b->con_total);
+    else
+        k_batch_contract<double2><<<g2, 256, 0, st>>>(b->d_entries, np, b->con_total);
+    if ((e = launched()))
+        return cuda_error(e, "batch contraction");
+    return FPG_OK;
+}
+
+} // namespace
+
+extern "C"
+{
+
+    int fpg_batch_create(int32_t dtype, fpg_batch **out)
+    {
+        if (!out)
+            return set_error(FPG_ERR_INVALID, "out is null");
+        *out = nullptr;
+        if (dtype != FPG_C128 && dtype != FPG_C64)
+            return set_error(FPG_ERR_INVALID, "dtype must be FPG_C128 or FPG_C64");
+        fpg_batch *b = new (std::nothrow) fpg_batch();
+        if (!b)
+            return set_error(FPG_ERR_NOMEM, "host allocation failed");
+        b->dtype = dtype;
+        cudaError_t e = cudaGetDevice(&b->device);
+        if (e != cudaSuccess)
+        {
+            delete b;
+            return cuda_error(e, "cudaGetDevice");
+        }
+        *out = b;
+        return FPG_OK;
+    }
+
+    int fpg_batch_add(fpg_batch *b, const fpg_operator *op, const void *coeffs, int64_t n_operators,
+                      const void *states, void *out, int64_t n_states)
+    {
+        if (!b || !op)
+            return set_error(FPG_ERR_INVALID, "null batch or operator");
+        if (n_operators < 1 || n_states < 1)
+            return set_error(FPG_ERR_INVALID, "n_operators and n_states must be >= 1");
+        if (op->P < 1)
+            return set_error(FPG_ERR_INVALID, "operator has no strings");
+        if (!coeffs || !states || !out)
+            return set_error(FPG_ERR_INVALID, "null array");
+        const uintptr_t al = b->dtype == FPG_C64 ? 8 : 16;
+        if ((uintptr_t)coeffs % al || (uintptr_t)states % al || (uintptr_t)out % al)
+            return set_error(FPG_ERR_INVALID, "complex arrays must be aligned to their element size");
+        if (op->device != b->device)
+            return set_error(FPG_ERR_INVALID, "operator and batch live on different devices");
+        b->problems.push_back(fpg_batch::Problem{op, coeffs, n_operators, states, out, n_states});
+        b->free_plan();
+        return FPG_OK;
+    }
+
+    int fpg_batch_plan(fpg_batch *b, const fpg_batch_tuning *tuning)
+    {
+        if (!b)
+            return set_error(FPG_ERR_INVALID, "batch is null");
+        if (b->problems.empty())
+            return set_error(FPG_ERR_INVALID, "batch is empty");
+        return do_plan(b, tuning ? *tuning : b->tuning);
+    }
+
+    int fpg_batch_run(fpg_batch *b, void *stream)
+    {
+        if (!b)
+            return set_error(FPG_ERR_INVALID, "batch is null");
+        if (!b->planned)
+            if (int rc = fpg_batch_plan(b, nullptr))
+                return rc;
+        return do_run(b, (cudaStream_t)stream);
+    }
+
+    int fpg_batch_run_graph(fpg_batch *b, void *stream)
+    {
+        if (!b)
+            return set_error(FPG_ERR_INVALID, "batch is null");
+        if (!b->planned)
+            if (int rc = fpg_batch_plan(b, nullptr))
+                return rc;
+        cudaStream_t st = (cudaStream_t)stream;
+        cudaError_t e;
+        if (!b->exec)
+        {
+            // capture on a private stream so a legacy-default caller stream works too
+            cudaStream_t cap;
+            if ((e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking)))
+                return cuda_error(e, "cudaStreamCreate");
+            if ((e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal)))
+            {
+                cudaStreamDestroy(cap);
+                return cuda_error(e, "cudaStreamBeginCapture");
+            }
+            const int rc = do_run(b, cap);
+            cudaGraph_t g = nullptr;
+            e = cudaStreamEndCapture(cap, &g);
+            cudaStreamDestroy(cap);
+            if (rc != FPG_OK)
+            {
+                if (g)
+                    cudaGraphDestroy(g);
+                return rc;
+            }
+            if (e != cudaSuccess)
+                return cuda_error(e, "cudaStreamEndCapture");
+            if ((e = cudaGraphInstantiate(&b->exec, g, 0)))
+            {
+                cudaGraphDestroy(g);
+                return cuda_error(e, "cudaGraphInstantiate");
+            }
+            b->graph = g;
+        }
+        if ((e = cudaGraphLaunch(b->exec, st)))
+            return cuda_error(e, "cudaGraphLaunch");
+        return FPG_OK;
+    }
+
+    int fpg_batch_autotune(fpg_batch *b, void *stream, fpg_batch_tuning *best, double *best_ms)
+    {
+        if (!b)
+            return set_error(FPG_ERR_INVALID, "batch is null");
+        if (b->problems.empty())
+            return set_error(FPG_ERR_INVALID, "batch is empty");
+        cudaStream_t st = (cudaStream_t)stream;
+        // candidate grid: CTA size x residency x work-item granularity
+        const int threads[] = {128, 256};
+        const int ctas[] = {2, 4, 8};
+        const int rows[] = {1 << 11, 1 << 13, 1 << 15};
+        fpg_batch_tuning top{};
+        double top_ms = 1e300;
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        for (int th : threads)
+            for (int cp : ctas)
+                for (int rw : rows)
+                {
+                    const fpg_batch_tuning cand{th, cp, rw};
+                    if (int rc = do_plan(b, cand))
+                    {
+                        cudaEventDestroy(e0);
+                        cudaEventDestroy(e1);
+                        return rc;
+                    }
+                    if (int rc = do_run(b, st)) // warm-up
+                    {
+                        cudaEventDestroy(e0);
+                        cudaEventDestroy(e1);
+                        return rc;
+                    }
+                    cudaEventRecord(e0, st);
+                    const int reps = 2;
+                    for (int r = 0; r < reps; ++r)
+                        if (int rc = do_run(b, st))
+                        {
+                            cudaEventDestroy(e0);
+                            cudaEventDestroy(e1);
+                            return rc;
+                        }
+                    cudaEventRecord(e1, st);
+                    cudaEventSynchronize(e1);
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    ms /= reps;
+                    if (ms < top_ms)
+                    {
+                        top_ms = ms;
+                        top = cand;
+                    }
+                }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (int rc = do_plan(b, top))
+            return rc;
+        if (best)
+            *best = top;
+        if (best_ms)
+            *best_ms = top_ms;
+        return FPG_OK;
+    }
+
+    int fpg_batch_info(const fpg_batch *b, int64_t *n_problems, int64_t *n_items, fpg_batch_tuning *tuning)
+    {
+        if (!b)
+            return set_error(FPG_ERR_INVALID, "batch is null");
+        if (n_problems)
+            *n_problems = (int64_t)b->problems.size();
+        if (n_items)
+            *n_items = b->planned ? b->class_begin[kNumChunkClasses] : 0;
+        if (tuning)
+            *tuning = b->tuning;
+        return FPG_OK;
+    }
+
+    int fpg_batch_destroy(fpg_batch *b)
+    {
+        if (!b)
+            return FPG_OK;
+        b->free_plan();
+        delete b;
+        return FPG_OK;
+    }
+
+} // extern "C"

@@ -151,27 +151,6 @@ int encode_strings(const char *strings, int64_t P, int n, std::vector<StringRec>
 
 } // namespace fpg
 
-struct fpg_operator
-{
-    int n = 0;
-    int64_t P = 0;
-    int device = 0;
-    std::vector<StringRec> recs;
-    std::vector<int32_t> orig;
-    std::vector<Group> groups;
-    std::vector<Chunk> chunks;
-    std::vector<int> class_begin;
-    StringRec *d_recs = nullptr;
-    int32_t *d_orig = nullptr;
-    Group *d_groups = nullptr;
-    Chunk *d_chunks = nullptr;
-
-    DevOp dev() const
-    {
-        return DevOp{n, P, (int64_t)groups.size(), d_recs, d_orig, d_groups};
-    }
-};
-
 namespace
 {
 

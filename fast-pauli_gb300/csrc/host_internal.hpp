@@ -22,3 +22,25 @@ int encode_strings(const char *strings, int64_t P, int n, std::vector<StringRec>
                    std::vector<Group> &groups, std::vector<Chunk> &chunks, std::vector<int> &class_begin);
 
 } // namespace fpg
+
+// An encoded operator: host copies of the encoding and their device mirrors.
+struct fpg_operator
+{
+    int n = 0;
+    int64_t P = 0;
+    int device = 0;
+    std::vector<fpg::StringRec> recs;
+    std::vector<int32_t> orig;
+    std::vector<fpg::Group> groups;
+    std::vector<fpg::Chunk> chunks;
+    std::vector<int> class_begin; // chunks of class c: [class_begin[c], class_begin[c+1])
+    fpg::StringRec *d_recs = nullptr;
+    int32_t *d_orig = nullptr;
+    fpg::Group *d_groups = nullptr;
+    fpg::Chunk *d_chunks = nullptr;
+
+    fpg::DevOp dev() const
+    {
+        return fpg::DevOp{n, P, (int64_t)groups.size(), d_recs, d_orig, d_groups};
+    }
+};

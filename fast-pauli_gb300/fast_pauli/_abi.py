@@ -52,7 +52,24 @@ SIGNATURES = {
     "fpg_summed_apply": (ctypes.c_int, [_P, _P, _I64, _P, _P, _I64, _I32, _P]),
     "fpg_summed_apply_weighted": (ctypes.c_int, [_P, _P, _I64, _P, _P, _P, _I64, _I32, _P]),
     "fpg_summed_expect_noalloc": (ctypes.c_int, [ctypes.c_char_p, _I64, _I32, _P, _I64, _P, _P, _I64, _I32, _P]),
+    "fpg_batch_create": (ctypes.c_int, [_I32, ctypes.POINTER(_P)]),
+    "fpg_batch_add": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _I64]),
+    "fpg_batch_plan": (ctypes.c_int, [_P, _P]),
+    "fpg_batch_run": (ctypes.c_int, [_P, _P]),
+    "fpg_batch_run_graph": (ctypes.c_int, [_P, _P]),
+    "fpg_batch_autotune": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(ctypes.c_double)]),
+    "fpg_batch_info": (ctypes.c_int, [_P, _PI64, _PI64, _P]),
+    "fpg_batch_destroy": (ctypes.c_int, [_P]),
 }
+
+
+class BatchTuning(ctypes.Structure):
+    _fields_ = [("threads_per_cta", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
+                ("rows_per_item", ctypes.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {"threads_per_cta": self.threads_per_cta, "ctas_per_sm": self.ctas_per_sm,
+                "rows_per_item": self.rows_per_item}
 
 
 class FpgError(RuntimeError):
@@ -122,6 +139,60 @@ class Operator:
         if self._h:
             lib().fpg_operator_destroy(self._h)
             self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Owning handle of an fpg_batch; keeps the operators (and any arrays the
+    caller hands over in ``keep``) alive while the batch exists."""
+
+    def __init__(self, dtype: int):
+        self._h = _P()
+        self._keep: list = []
+        check(lib().fpg_batch_create(dtype, ctypes.byref(self._h)))
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def add(self, op: Operator, coeffs_ptr: int, n_operators: int, states_ptr: int, out_ptr: int, n_states: int,
+            keep=()) -> None:
+        self._keep.append(op)
+        self._keep.extend(keep)
+        check(lib().fpg_batch_add(self._h, op.handle, coeffs_ptr, n_operators, states_ptr, out_ptr, n_states))
+
+    def plan(self, tuning: "BatchTuning | None" = None) -> None:
+        check(lib().fpg_batch_plan(self._h, ctypes.byref(tuning) if tuning is not None else None))
+
+    def run(self, stream) -> None:
+        check(lib().fpg_batch_run(self._h, stream))
+
+    def run_graph(self, stream) -> None:
+        check(lib().fpg_batch_run_graph(self._h, stream))
+
+    def autotune(self, stream) -> tuple[dict, float]:
+        best = BatchTuning()
+        ms = ctypes.c_double()
+        check(lib().fpg_batch_autotune(self._h, stream, ctypes.byref(best), ctypes.byref(ms)))
+        return best.as_dict(), ms.value
+
+    def info(self) -> tuple[int, int, dict]:
+        n = ctypes.c_int64()
+        it = ctypes.c_int64()
+        t = BatchTuning()
+        check(lib().fpg_batch_info(self._h, ctypes.byref(n), ctypes.byref(it), ctypes.byref(t)))
+        return n.value, it.value, t.as_dict()
+
+    def close(self) -> None:
+        if self._h:
+            lib().fpg_batch_destroy(self._h)
+            self._h = _P()
+        self._keep = []
 
     def __del__(self):
         try:

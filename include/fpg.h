@@ -155,6 +155,43 @@ int fpg_summed_apply(const fpg_operator *op, const void *coeffs, int64_t n_opera
 int fpg_summed_apply_weighted(const fpg_operator *op, const void *coeffs, int64_t n_operators, const void *states,
                               const void *data, void *out, int64_t n_states, int32_t dtype, void *stream);
 
+/* ------------------------------------------------------------------------
+ * Batches: many expectation problems of uneven size (qubits, strings,
+ * states, operators) run as one persistent work-queue launch per chunk class
+ * plus a reduction and a contraction -- no allocation at run time, so a run
+ * can be captured into a CUDA graph.  No counterpart in the reference (its
+ * equivalent is a loop of PauliOp/SummedPauliOp::expectation_value calls,
+ * __pauli_op.hpp:482-549, __summed_pauli_op.hpp:520-614).
+ * Each problem: out(K,S) = sum_j coeffs(j,k) <psi_t|P_j|psi_t>; a run
+ * OVERWRITES the outputs (so repeated runs and autotuning are idempotent).
+ * All arrays are device arrays of the batch's dtype and must stay valid
+ * while the batch is used.  Runs of one batch must not overlap on the GPU.
+ * ------------------------------------------------------------------------ */
+typedef struct fpg_batch fpg_batch;
+
+typedef struct fpg_batch_tuning
+{
+    int32_t threads_per_cta; /* 128 or 256                                          */
+    int32_t ctas_per_sm;     /* CTAs per SM of each persistent grid, 1..8          */
+    int32_t rows_per_item;   /* rows of one work item, power of two >= 32          */
+} fpg_batch_tuning;
+
+int fpg_batch_create(int32_t dtype, fpg_batch **out);
+int fpg_batch_add(fpg_batch *batch, const fpg_operator *op, const void *coeffs, int64_t n_operators,
+                  const void *states, void *out, int64_t n_states);
+/* Build the work queue and per-problem partial tables (allocates device memory).
+ * tuning NULL: the batch's current tuning (defaults 256 / 4 / 4096). */
+int fpg_batch_plan(fpg_batch *batch, const fpg_batch_tuning *tuning);
+/* Enqueue one run on stream (plans first if needed). */
+int fpg_batch_run(fpg_batch *batch, void *stream);
+/* Same, through a CUDA graph captured on first use and replayed afterwards. */
+int fpg_batch_run_graph(fpg_batch *batch, void *stream);
+/* Times every candidate tuning on this batch (runs it 3x per candidate),
+ * re-plans with the fastest and reports it. */
+int fpg_batch_autotune(fpg_batch *batch, void *stream, fpg_batch_tuning *best, double *best_ms);
+int fpg_batch_info(const fpg_batch *batch, int64_t *n_problems, int64_t *n_items, fpg_batch_tuning *tuning);
+int fpg_batch_destroy(fpg_batch *batch);
+
 /*
  * fpg_summed_expect_noalloc: the same result as fpg_summed_expect
  * (out(K,S) += sum_j coeffs(j,k) <psi_t|P_j|psi_t>), for callers that cannot
