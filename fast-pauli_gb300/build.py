@@ -29,7 +29,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["k_expect.cu", "k_apply.cu", "k_contract.cu", "k_contract_tc.cu", "k_noalloc.cu", "batch.cu"]
-CPP_SOURCES = ["capi.cpp"]
+CPP_SOURCES = ["capi.cpp", "server.cpp"]
 
 
 def _cuda_include() -> str:
@@ -82,13 +82,13 @@ def build_lib(force: bool = False, verbose_ptxas: bool = False) -> str:
         o = os.path.join(OBJ_DIR, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-Wextra", "-I", CSRC, "-I", ABI_INC,
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-Wall", "-Wextra", "-I", CSRC, "-I", ABI_INC,
                          "-I", _cuda_include(), "-c", s, "-o", o])
     with ThreadPoolExecutor(max_workers=max(1, min(8, os.cpu_count() or 1))) as ex:
         list(ex.map(_run, jobs))
     if force or jobs or _stale(LIB, objs):
         tmp = LIB + f".tmp{os.getpid()}"
-        _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"])
+        _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-Xcompiler", "-pthread"])
         os.replace(tmp, LIB)
     return LIB
 

@@ -289,6 +289,31 @@ int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int6
 
 } // namespace
 
+namespace fpg
+{
+// Upper bound of the stream-ordered scratch one fpg_summed_expect (weighted =
+// false) or fpg_summed_apply_weighted (weighted = true) call draws.
+size_t request_scratch_bytes(const fpg_operator *op, int64_t K, int64_t S, bool fp32, bool weighted)
+{
+    const size_t P = (size_t)op->P;
+    if (weighted)
+    {
+        const size_t csz = fp32 ? 8 : 16;
+        size_t b = 2 * P * (size_t)S * csz;
+        if (fp32)
+            b += tc_workspace_bytes(2 * op->P, S, K);
+        return b + 4096;
+    }
+    const ExpectPlan plan = plan_expect(op, S, fp32, nullptr);
+    size_t b = P * (size_t)S * sizeof(double);
+    if (plan.n_splits > 1)
+        b += (size_t)plan.n_splits * P * (size_t)S * sizeof(double);
+    if (fp32)
+        b += tc_workspace_bytes(2 * K, S, op->P);
+    return b + 4096;
+}
+} // namespace fpg
+
 // ---------------------------------------------------------------------------
 // entry points
 // ---------------------------------------------------------------------------

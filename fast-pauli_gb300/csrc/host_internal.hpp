@@ -23,6 +23,15 @@ int encode_strings(const char *strings, int64_t P, int n, std::vector<StringRec>
 
 } // namespace fpg
 
+struct fpg_operator;
+
+namespace fpg
+{
+// Upper bound of the scratch bytes one expectation (weighted = false) or
+// apply_weighted (weighted = true) call draws from the stream-ordered pool.
+size_t request_scratch_bytes(const fpg_operator *op, int64_t K, int64_t S, bool fp32, bool weighted);
+} // namespace fpg
+
 // An encoded operator: host copies of the encoding and their device mirrors.
 struct fpg_operator
 {

@@ -63,6 +63,42 @@ SIGNATURES = {
 }
 
 
+FPG_REQ_EXPECT = 0
+FPG_REQ_APPLY_WEIGHTED = 1
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("reserved", ctypes.c_int32), ("op", _P), ("coeffs", _P),
+                ("n_operators", ctypes.c_int64), ("states", _P), ("data", _P), ("out", _P),
+                ("n_states", ctypes.c_int64)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("dtype", ctypes.c_int32), ("n_slots", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_int64),
+                ("max_queue", ctypes.c_int64)]
+
+
+class TicketInfo(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("reserved", ctypes.c_int32), ("scratch_bytes", ctypes.c_int64),
+                ("submit_us", ctypes.c_double), ("start_us", ctypes.c_double), ("done_us", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_int64), ("failed", ctypes.c_int64), ("refused", ctypes.c_int64),
+                ("queued", ctypes.c_int64), ("peak_running", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("peak_reserved_bytes", ctypes.c_int64)]
+
+
+SIGNATURES.update({
+    "fpg_server_create": (ctypes.c_int, [ctypes.POINTER(ServerConfig), ctypes.POINTER(_P)]),
+    "fpg_server_submit": (ctypes.c_int, [_P, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]),
+    "fpg_server_wait": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.c_int32, ctypes.POINTER(TicketInfo)]),
+    "fpg_server_release": (ctypes.c_int, [_P, ctypes.c_uint64]),
+    "fpg_server_stats": (ctypes.c_int, [_P, ctypes.POINTER(ServerStats)]),
+    "fpg_server_destroy": (ctypes.c_int, [_P]),
+})
+
+
 class BatchTuning(ctypes.Structure):
     _fields_ = [("threads_per_cta", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
                 ("rows_per_item", ctypes.c_int32)]
@@ -138,6 +174,52 @@ class Operator:
     def close(self) -> None:
         if self._h:
             lib().fpg_operator_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Owning handle of an fpg_server (device-resident request loop)."""
+
+    def __init__(self, dtype: int, n_slots: int = 4, hbm_budget_bytes: int = 8 << 30, max_queue: int = 0):
+        self._h = _P()
+        cfg = ServerConfig(dtype, n_slots, hbm_budget_bytes, max_queue)
+        check(lib().fpg_server_create(ctypes.byref(cfg), ctypes.byref(self._h)))
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def submit(self, kind: int, op: "Operator", coeffs_ptr: int, n_operators: int, states_ptr: int, out_ptr: int,
+               n_states: int, data_ptr: int = 0) -> int:
+        req = Request(kind, 0, op.handle, coeffs_ptr, n_operators, states_ptr, data_ptr or None, out_ptr, n_states)
+        t = ctypes.c_uint64()
+        check(lib().fpg_server_submit(self._h, ctypes.byref(req), ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1) -> dict:
+        info = TicketInfo()
+        check(lib().fpg_server_wait(self._h, ticket, timeout_ms, ctypes.byref(info)))
+        return {"status": info.status, "scratch_bytes": info.scratch_bytes, "submit_us": info.submit_us,
+                "start_us": info.start_us, "done_us": info.done_us}
+
+    def release(self, ticket: int) -> None:
+        check(lib().fpg_server_release(self._h, ticket))
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        check(lib().fpg_server_stats(self._h, ctypes.byref(s)))
+        return {"completed": s.completed, "failed": s.failed, "refused": s.refused, "queued": s.queued,
+                "peak_running": s.peak_running, "peak_reserved_bytes": s.peak_reserved_bytes}
+
+    def close(self) -> None:
+        if self._h:
+            lib().fpg_server_destroy(self._h)
             self._h = _P()
 
     def __del__(self):

@@ -192,6 +192,71 @@ int fpg_batch_autotune(fpg_batch *batch, void *stream, fpg_batch_tuning *best, d
 int fpg_batch_info(const fpg_batch *batch, int64_t *n_problems, int64_t *n_items, fpg_batch_tuning *tuning);
 int fpg_batch_destroy(fpg_batch *batch);
 
+/* ------------------------------------------------------------------------
+ * Serving: a device-resident request loop with continuous admission.  No
+ * counterpart in the reference.  Requests reference resident operators and
+ * device arrays; a scheduler thread admits queued requests as soon as a slot
+ * (one CUDA stream) is free and the request's scratch fits the remaining HBM
+ * budget, so requests arriving while others run are started immediately and
+ * overlap on the device.  A request needing more than the whole budget, or
+ * arriving at a full queue, is refused with FPG_ERR_BUSY.  Outputs are
+ * overwritten.  Results do not depend on the mix (same kernels as alone).
+ * ------------------------------------------------------------------------ */
+enum fpg_request_kind
+{
+    FPG_REQ_EXPECT = 0,        /* out(K,S) = sum_j coeffs(j,k) <psi_t|P_j|psi_t>               */
+    FPG_REQ_APPLY_WEIGHTED = 1 /* out(D,S) = sum_j (sum_k coeffs(j,k) data(k,t)) P_j psi_t   */
+};
+
+typedef struct fpg_request
+{
+    int32_t kind;
+    int32_t reserved;
+    const fpg_operator *op;
+    const void *coeffs; /* (n_strings, n_operators) complex, device             */
+    int64_t n_operators;
+    const void *states; /* (2^n, n_states) complex, device                        */
+    const void *data;   /* (n_operators, n_states) real, APPLY_WEIGHTED only      */
+    void *out;          /* (K, S) or (2^n, S) complex, device                     */
+    int64_t n_states;
+} fpg_request;
+
+typedef struct fpg_server_config
+{
+    int32_t dtype;            /* FPG_C128 or FPG_C64 for every request            */
+    int32_t n_slots;          /* concurrent requests (streams), 1..64             */
+    int64_t hbm_budget_bytes; /* scratch memory all running requests may hold   */
+    int64_t max_queue;        /* queued requests before refusing (<= 0: 2^20)   */
+} fpg_server_config;
+
+typedef struct fpg_ticket_info
+{
+    int32_t status; /* 2 done, 3 failed                                        */
+    int32_t reserved;
+    int64_t scratch_bytes;
+    double submit_us, start_us, done_us; /* steady clock, microseconds since server creation */
+} fpg_ticket_info;
+
+typedef struct fpg_server_stats_t
+{
+    int64_t completed, failed, refused, queued;
+    int32_t peak_running;
+    int32_t reserved;
+    int64_t peak_reserved_bytes;
+} fpg_server_stats_t;
+
+typedef struct fpg_server fpg_server;
+
+int fpg_server_create(const fpg_server_config *config, fpg_server **out);
+int fpg_server_submit(fpg_server *server, const fpg_request *request, uint64_t *ticket);
+/* Block until the ticket finishes (timeout_ms < 0: no limit); fills info. */
+int fpg_server_wait(fpg_server *server, uint64_t ticket, int32_t timeout_ms, fpg_ticket_info *info);
+/* Forget a finished ticket. */
+int fpg_server_release(fpg_server *server, uint64_t ticket);
+int fpg_server_stats(fpg_server *server, fpg_server_stats_t *stats);
+/* Drains queued and running requests, then stops the scheduler. */
+int fpg_server_destroy(fpg_server *server);
+
 /*
  * fpg_summed_expect_noalloc: the same result as fpg_summed_expect
  * (out(K,S) += sum_j coeffs(j,k) <psi_t|P_j|psi_t>), for callers that cannot
