@@ -420,6 +420,189 @@ def run_reference(args, rank, world):
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def _cfg4_problems(seed=1004, count=256):
+    """Configuration 4: n ~ U{8..20}, strings log-uniform in [16, 4096]
+    (uniform random strings), states ~ U{1..256}."""
+    import numpy as np
+
+    import oracle
+
+    rng = np.random.default_rng(seed)
+    probs = []
+    for _ in range(count):
+        n = int(rng.integers(8, 21))
+        P = int(np.exp(rng.uniform(np.log(16), np.log(4096))))
+        S = int(rng.integers(1, 257))
+        strings = oracle.uniform_strings(rng, n, P)
+        c = rng.standard_normal(P) + 1j * rng.standard_normal(P)
+        probs.append((n, strings, c, S))
+    return probs
+
+
+def run_batch(args):
+    """Configuration 4: 256 uneven PauliOp.expectation_value problems in one
+    persistent, graph-captured launch (tuning from the autotuner, tuned on the
+    problems with n <= 14) versus 256 separate plain launches."""
+    import numpy as np
+    import torch
+
+    import oracle
+    from fast_pauli import _abi
+
+    torch.cuda.set_device(0)
+    L = _abi.lib()
+    probs = _cfg4_problems()
+    stream = _stream_handle()
+    g = torch.Generator(device="cuda").manual_seed(4)
+    items = []
+    for n, strings, c, S in probs:
+        D = 1 << n
+        psi = torch.complex(torch.randn(D, S, device="cuda", generator=g),
+                            torch.randn(D, S, device="cuda", generator=g))
+        psi /= torch.linalg.vector_norm(psi.to(torch.complex128), dim=0, keepdim=True).to(torch.float32)
+        op = _abi.Operator(strings)
+        dc = torch.from_numpy(c.reshape(-1, 1)).to(torch.complex64).cuda()
+        items.append(dict(n=n, P=len(strings), S=S, psi=psi, op=op, c=dc,
+                          out_b=torch.zeros((1, S), dtype=torch.complex64, device="cuda"),
+                          out_p=torch.zeros((1, S), dtype=torch.complex64, device="cuda")))
+    terms = sum(it["P"] * (1 << it["n"]) * it["S"] for it in items)
+    # autotune on the small problems (a proxy: same kernels, a fraction of the time)
+    proxy = _abi.Batch(_abi.FPG_C64)
+    for it in items:
+        if it["n"] <= 14:
+            proxy.add(it["op"], it["c"].data_ptr(), 1, it["psi"].data_ptr(), it["out_b"].data_ptr(), it["S"])
+    best, best_ms = proxy.autotune(stream)
+    proxy.close()
+    batch = _abi.Batch(_abi.FPG_C64)
+    for it in items:
+        batch.add(it["op"], it["c"].data_ptr(), 1, it["psi"].data_ptr(), it["out_b"].data_ptr(), it["S"])
+    batch.plan(_abi.BatchTuning(best["threads_per_cta"], best["ctas_per_sm"], best["rows_per_item"],
+                                best["tile_mb"]))
+    n0 = _abi.kernel_launches()
+    t_batch = time_device(lambda: batch.run_graph(stream), args.steps, max(1, args.warmup))
+    launches_batch = (_abi.kernel_launches() - n0) / (args.steps + max(1, args.warmup))
+
+    def plain():
+        for it in items:
+            it["out_p"].zero_()
+            _abi.check(L.fpg_summed_expect(it["op"].handle, it["c"].data_ptr(), 1, it["psi"].data_ptr(),
+                                           it["out_p"].data_ptr(), it["S"], _abi.FPG_C64, stream))
+
+    n0 = _abi.kernel_launches()
+    t_plain = time_device(plain, max(1, args.steps // 2), 1)
+    launches_plain = (_abi.kernel_launches() - n0) / (max(1, args.steps // 2) + 1)
+    # agreement batch vs plain, and the smallest problems vs the CPU oracle
+    err_bp = max(normwise_np(it["out_b"].cpu().numpy(), it["out_p"].cpu().numpy()) for it in items)
+    small = sorted(range(len(items)), key=lambda i: items[i]["P"] * (1 << items[i]["n"]) * items[i]["S"])[:6]
+    err_or = 0.0
+    cpu_terms, cpu_t = 0, 0.0
+    for i in small:
+        n, strings, c, S = probs[i]
+        psi = items[i]["psi"].cpu().numpy().astype(np.complex128)
+        t0 = time.perf_counter()
+        want = oracle.op_expectation(strings, c, psi)
+        cpu_t += time.perf_counter() - t0
+        cpu_terms += len(strings) * (1 << n) * S
+        err_or = max(err_or, normwise_np(items[i]["out_b"].cpu().numpy()[0], want))
+    hbm, _ = _peaks()
+    return {"metric": METRIC, "workload": "config 4: 256 PauliOp.expectation_value, n~U{8..20}, P log-uniform "
+                                          "16..4096 uniform strings, S~U{1..256}, complex64",
+            "value": terms / t_batch, "unit": UNIT, "ms_per_step": t_batch * 1e3, "steps": args.steps,
+            "plain_value": terms / t_plain, "plain_ms_per_step": t_plain * 1e3, "speedup_vs_plain": t_plain / t_batch,
+            "terms": terms, "streaming_equiv_frac_of_hbm": terms * 8 / t_batch / 1e9 / hbm,
+            "launches_per_step": launches_batch, "plain_launches_per_step": launches_plain,
+            "tuning": best, "autotune_proxy_ms": best_ms,
+            "max_normwise_diff_batch_vs_plain": err_bp, "max_normwise_err_vs_oracle_smallest6": err_or,
+            "cpu_baseline": {"value": cpu_terms / cpu_t, "unit": UNIT, "cores": oracle.max_threads(),
+                             "kind": "port", "sample": "the 6 smallest problems"}}
+
+
+def normwise_np(got, want):
+    import numpy as np
+
+    den = np.abs(want).max()
+    return float(np.abs(got - want).max() / den) if den > 0 else float(np.abs(got - want).max())
+
+
+def run_serve(args):
+    """Configuration 5: Poisson arrivals of expectation_value / apply_weighted
+    requests (n ~ U{10..max_n}, strings log-uniform 32..2048, S ~ U{1..64},
+    K log-uniform 1..64, complex64) against the serving loop (continuous
+    admission, 8 slots, HBM budget) and against the plain per-request path
+    (one slot, first come first served).  Latency = completion - arrival."""
+    import numpy as np
+    import torch
+
+    import oracle
+    from fast_pauli import _abi
+
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(1005)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    n_req = args.requests
+    reqs = []
+    for i in range(n_req):
+        n = int(rng.integers(10, args.max_n + 1))
+        P = int(np.exp(rng.uniform(np.log(32), np.log(2048))))
+        S = int(rng.integers(1, 65))
+        K = int(np.exp(rng.uniform(0, np.log(64))))
+        kind = _abi.FPG_REQ_EXPECT if rng.random() < 0.5 else _abi.FPG_REQ_APPLY_WEIGHTED
+        strings = oracle.uniform_strings(rng, n, P)
+        D = 1 << n
+        psi = torch.complex(torch.randn(D, S, device="cuda", generator=g),
+                            torch.randn(D, S, device="cuda", generator=g))
+        psi /= torch.linalg.vector_norm(psi, dim=0, keepdim=True)
+        h = torch.complex(torch.randn(P, K, device="cuda", generator=g), torch.randn(P, K, device="cuda", generator=g))
+        data = torch.randn(K, S, device="cuda", generator=g)
+        out_shape = (K, S) if kind == _abi.FPG_REQ_EXPECT else (D, S)
+        reqs.append(dict(n=n, P=P, S=S, K=K, kind=kind, op=_abi.Operator(strings), psi=psi, h=h, data=data,
+                         out=torch.empty(out_shape, dtype=torch.complex64, device="cuda")))
+    torch.cuda.synchronize()
+    gaps = rng.exponential(1.0 / args.rate, size=n_req)
+
+    def serve(n_slots):
+        srv = _abi.Server(_abi.FPG_C64, n_slots=n_slots, hbm_budget_bytes=args.budget_gb << 30)
+        # warm-up: one small request
+        r0 = min(reqs, key=lambda r: r["P"] << r["n"])
+        srv.wait(srv.submit(r0["kind"], r0["op"], r0["h"].data_ptr(), r0["K"], r0["psi"].data_ptr(),
+                            r0["out"].data_ptr(), r0["S"], r0["data"].data_ptr()))
+        tickets = []
+        t0 = time.perf_counter()
+        arrive = t0
+        for r, gap in zip(reqs, gaps):
+            arrive += gap
+            while time.perf_counter() < arrive:
+                time.sleep(min(1e-4, max(0.0, arrive - time.perf_counter())))
+            tickets.append(srv.submit(r["kind"], r["op"], r["h"].data_ptr(), r["K"], r["psi"].data_ptr(),
+                                      r["out"].data_ptr(), r["S"], r["data"].data_ptr()))
+        infos = [srv.wait(t) for t in tickets]
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        lat = np.array([(i["done_us"] - i["submit_us"]) / 1e3 for i in infos])
+        return lat, wall, st
+
+    terms = sum(r["P"] * (1 << r["n"]) * r["S"] for r in reqs)
+    out = {"metric": "serving latency ms / amplitude-terms/s",
+           "workload": f"config 5: {n_req} requests, Poisson rate {args.rate}/s, n~U{{10..{args.max_n}}}, "
+                       "P log-uniform 32..2048 uniform strings, S~U{1..64}, K log-uniform 1..64, "
+                       "50/50 expectation_value / apply_weighted, complex64"}
+    for name, slots in (("served", args.slots), ("plain_per_request", 1)):
+        lat, wall, st = serve(slots)
+        buckets = {}
+        ns = np.array([r["n"] for r in reqs])
+        for lo, hi in ((10, 14), (15, 20), (21, 24)):
+            m = (ns >= lo) & (ns <= hi)
+            if m.any():
+                buckets[f"n{lo}-{hi}"] = {"count": int(m.sum()), "p50_ms": float(np.percentile(lat[m], 50)),
+                                          "p99_ms": float(np.percentile(lat[m], 99))}
+        out[name] = {"slots": slots, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                     "throughput_terms_per_s": terms / wall, "requests_per_s": n_req / wall, "wall_s": wall,
+                     "by_n": buckets, "peak_running": st["peak_running"],
+                     "peak_reserved_gb": st["peak_reserved_bytes"] / 2**30}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -430,11 +613,23 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-mixed", action="store_true")
+    ap.add_argument("--workload", default="summed", choices=["summed", "batch", "serve"],
+                    help="summed: configuration 2 (default line); batch: configuration 4; serve: configuration 5")
+    ap.add_argument("--requests", type=int, default=200, help="serve: number of requests")
+    ap.add_argument("--rate", type=float, default=50.0, help="serve: Poisson arrival rate (requests/s)")
+    ap.add_argument("--max-n", type=int, default=24, help="serve: largest qubit count")
+    ap.add_argument("--slots", type=int, default=8, help="serve: concurrent request slots")
+    ap.add_argument("--budget-gb", type=int, default=64, help="serve: HBM budget for request scratch")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     dist = None
+    if args.workload != "summed" and args.impl == "ours":
+        if rank == 0:
+            line = run_batch(args) if args.workload == "batch" else run_serve(args)
+            print(json.dumps(line), flush=True)
+        return
     if args.impl == "reference":
         line = run_reference(args, rank, world)
         if line is not None:

@@ -162,7 +162,7 @@ struct fpg_batch
         int64_t S;
     };
     std::vector<Problem> problems;
-    fpg_batch_tuning tuning{256, 4, 1 << 12};
+    fpg_batch_tuning tuning{256, 4, 1 << 12, 40};
     bool planned = false;
     // device state of the plan
     BatchEntry *d_entries = nullptr;
@@ -272,6 +272,8 @@ int do_plan(fpg_batch *b, const fpg_batch_tuning &t)
         return set_error(FPG_ERR_INVALID, "ctas_per_sm must be in [1, 8]");
     if (t.rows_per_item < 32 || (t.rows_per_item & (t.rows_per_item - 1)))
         return set_error(FPG_ERR_INVALID, "rows_per_item must be a power of two >= 32");
+    if (t.tile_mb < 1)
+        return set_error(FPG_ERR_INVALID, "tile_mb must be >= 1");
     b->free_plan();
     const int np = (int)b->problems.size();
     // largest problems first
@@ -303,7 +305,7 @@ int do_plan(fpg_batch *b, const fpg_batch_tuning &t)
         e.P = op->P;
         e.K = p.K;
         e.n = op->n;
-        e.TC = std::min(tc_for(p.S), t.threads_per_cta);
+        e.TC = column_lanes_for_l2(std::min(tc_for(p.S), t.threads_per_cta), op->n, b->dtype == FPG_C64 ? 8 : 16, (int64_t)t.tile_mb << 20);
         const int64_t NB = op->n >= 5 ? ((int64_t)1 << (op->n - 5)) : 1;
         const int64_t blocks_per_item = std::max<int64_t>(1, t.rows_per_item / 32);
         e.n_splits = (int32_t)std::max<int64_t>(1, std::min<int64_t>(64, NB / blocks_per_item));
@@ -529,8 +531,9 @@ extern "C"
         cudaStream_t st = (cudaStream_t)stream;
         // candidate grid: CTA size x residency x work-item granularity
         const int threads[] = {128, 256};
-        const int ctas[] = {2, 4, 8};
-        const int rows[] = {1 << 11, 1 << 13, 1 << 15};
+        const int ctas[] = {4, 8};
+        const int rows[] = {1 << 11, 1 << 13};
+        const int tiles[] = {16, 48};
         fpg_batch_tuning top{};
         double top_ms = 1e300;
         cudaEvent_t e0, e1;
@@ -539,8 +542,9 @@ extern "C"
         for (int th : threads)
             for (int cp : ctas)
                 for (int rw : rows)
+                    for (int tmb : tiles)
                 {
-                    const fpg_batch_tuning cand{th, cp, rw};
+                    const fpg_batch_tuning cand{th, cp, rw, tmb};
                     if (int rc = do_plan(b, cand))
                     {
                         cudaEventDestroy(e0);

@@ -248,7 +248,7 @@ ExpectPlan plan_expect(const fpg_operator *op, int64_t S, bool fp32, const void 
     ExpectPlan p{};
     p.V = (fp32 && (S % 2 == 0) && (((uintptr_t)psi) % 16 == 0)) ? 2 : 1;
     const int64_t lanes = (S + p.V - 1) / p.V;
-    p.TC = pick_tc(lanes);
+    p.TC = column_lanes_for_l2(pick_tc(lanes), op->n, p.V * (fp32 ? 8 : 16), kColumnTileBytes);
     p.n_ctiles = (int)((S + (int64_t)p.TC * p.V - 1) / ((int64_t)p.TC * p.V));
     const int TR = 256 / p.TC;
     const int64_t n_chunks = (int64_t)op->chunks.size();

@@ -77,6 +77,21 @@ struct ChunkClass
 extern const ChunkClass kChunkClasses[kNumChunkClasses];
 int chunk_class_for(int n_even, int n_odd); // smallest class covering, -1 if none
 
+// Column tiling for L2 residency.  All chunks of a launch sweep the same
+// column tile (2^n rows x TC lanes x bytes per lane) before moving to the
+// next, so the state is read from DRAM about once per launch when the tile
+// fits comfortably in the 126 MB L2; the partner rows (i ^ x) of random
+// strings then hit L2 too.  Narrow the tile (halve TC) until it fits the
+// budget, keeping at least 32 bytes per row access (one sector).
+constexpr int64_t kColumnTileBytes = int64_t(40) << 20;
+inline int column_lanes_for_l2(int tc, int n, int bytes_per_lane, int64_t budget)
+{
+    const int min_tc = bytes_per_lane >= 32 ? 1 : 32 / bytes_per_lane;
+    while (tc > min_tc && (int64_t(1) << n) * (int64_t)tc * bytes_per_lane > budget)
+        tc >>= 1;
+    return tc;
+}
+
 struct ExpectPlan
 {
     int TC;           // column lanes per CTA (power of two <= 32)

@@ -9,7 +9,11 @@
 //   * apply_weighted: A = [Re H; Im H] (2P x K), B = X^T (S x K), C (2P x S).
 // Split precision (3xTF32): every operand x = x_hi + x_lo with
 // x_hi = tf32(x) (round to nearest) and x_lo = tf32(x - x_hi); the product is
-// A_hi B_hi + A_hi B_lo + A_lo B_hi, accumulated in float32 in TMEM.
+// A_hi B_hi + A_hi B_lo + A_lo B_hi, accumulated in float32 in TMEM over one
+// 32-deep k segment per CTA (grid z = segment); the finishing kernels sum the
+// segments in float64.  Long float32 accumulations over thousands of terms
+// with cancellation (e.g. a PauliOp with 4096 strings, K = 1) otherwise lose
+// ~1e-5 relative accuracy.
 //
 // Data movement: a prep kernel writes each operand in the canonical K-major,
 // no-swizzle core-matrix layout (8 rows x 16 bytes per core matrix), one
@@ -193,11 +197,18 @@ __global__ void k_prep_b_weighted(const float *__restrict__ X, int64_t K, int64_
 }
 
 // ------------------------------------------------------------------- GEMM
-// C (rows_pad x cols_pad, row-major float32) = A B^T for one 128x128 tile per CTA.
+// One 128x128 tile of one k segment per CTA (blockIdx.z = segment of
+// seg_chunks 32-deep chunks): C[z] (rows_pad x cols_pad, row-major float32)
+// = A B^T restricted to the segment.  Accumulation is float32 inside a
+// segment only; the segments are summed in float64 by the finishing kernels.
 __global__ void __launch_bounds__(128, 1)
     k_gemm_tf32x3(const float *__restrict__ a_hi, const float *__restrict__ a_lo, const float *__restrict__ b_hi,
-                  const float *__restrict__ b_lo, int64_t kchunks, int64_t cols_pad, float *__restrict__ C)
+                  const float *__restrict__ b_lo, int64_t kchunks, int64_t seg_chunks, int64_t rows_pad,
+                  int64_t cols_pad, float *__restrict__ C)
 {
+    const int64_t kb = (int64_t)blockIdx.z * seg_chunks;
+    const int64_t nk = min(kchunks, kb + seg_chunks) - kb; // chunks of this segment (>= 1)
+    C += (int64_t)blockIdx.z * rows_pad * cols_pad;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     // 1024-byte aligned ring of stages, then barriers
     unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -237,21 +248,21 @@ __global__ void __launch_bounds__(128, 1)
     if (threadIdx.x == 0)
     {
         const float *srcs[4];
+        // local chunk kc of this segment = global chunk kb + kc
         auto issue = [&](int64_t kc, int s) {
-            srcs[0] = a_hi + (mt * kchunks + kc) * (BLOCK_BYTES / 4);
-            srcs[1] = a_lo + (mt * kchunks + kc) * (BLOCK_BYTES / 4);
-            srcs[2] = b_hi + (nt * kchunks + kc) * (BLOCK_BYTES / 4);
-            srcs[3] = b_lo + (nt * kchunks + kc) * (BLOCK_BYTES / 4);
+            srcs[0] = a_hi + (mt * kchunks + kb + kc) * (BLOCK_BYTES / 4);
+            srcs[1] = a_lo + (mt * kchunks + kb + kc) * (BLOCK_BYTES / 4);
+            srcs[2] = b_hi + (nt * kchunks + kb + kc) * (BLOCK_BYTES / 4);
+            srcs[3] = b_lo + (nt * kchunks + kb + kc) * (BLOCK_BYTES / 4);
             mbar_expect_tx(&full[s], STAGE_BYTES);
             for (int q = 0; q < 4; ++q)
                 bulk_copy_g2s(smem + s * STAGE_BYTES + q * BLOCK_BYTES, srcs[q], BLOCK_BYTES, &full[s]);
         };
         uint32_t full_phase[NSTAGE] = {0, 0}, empty_phase[NSTAGE] = {0, 0};
         int64_t issued = 0;
-        for (; issued < kchunks && issued < NSTAGE; ++issued)
+        for (; issued < nk && issued < NSTAGE; ++issued)
             issue(issued, (int)issued);
-        int64_t committed = 0;
-        for (int64_t kc = 0; kc < kchunks && ok; ++kc)
+        for (int64_t kc = 0; kc < nk && ok; ++kc)
         {
             const int s = (int)(kc % NSTAGE);
             if (!mbar_wait(&full[s], full_phase[s]))
@@ -276,8 +287,7 @@ __global__ void __launch_bounds__(128, 1)
                 mma_tf32(tmem, dal, dbh, 1u);
             }
             mma_commit(&empty[s]);
-            committed = kc + 1;
-            if (issued < kchunks)
+            if (issued < nk)
             {
                 // stage s is refilled once the MMAs that read it have completed
                 if (!mbar_wait(&empty[s], empty_phase[s]))
@@ -299,7 +309,6 @@ __global__ void __launch_bounds__(128, 1)
             for (int s = 0; s < NSTAGE; ++s)
                 (void)mbar_wait(&full[s], full_phase[s]);
         }
-        (void)committed;
         *status = ok ? 1 : 0;
     }
     __syncthreads();
@@ -345,30 +354,40 @@ __global__ void __launch_bounds__(128, 1)
 }
 
 // -------------------------------------------------------------- epilogues
+// Segments are summed in float64, in segment order.
+__device__ __forceinline__ double seg_sum(const float *__restrict__ C, int64_t nseg, int64_t seg_stride, int64_t idx)
+{
+    double s = 0.0;
+    for (int64_t z = 0; z < nseg; ++z)
+        s += (double)C[z * seg_stride + idx];
+    return s;
+}
+
 // expectation: out[k][t] += (C[k][t], C[K+k][t])   (complex64 out)
-__global__ void k_finish_expect(const float *__restrict__ C, int64_t cols_pad, int64_t K, int64_t S,
-                                float2 *__restrict__ out)
+__global__ void k_finish_expect(const float *__restrict__ C, int64_t nseg, int64_t seg_stride, int64_t cols_pad,
+                                int64_t K, int64_t S, float2 *__restrict__ out)
 {
     const int64_t total = K * S;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
     {
         const int64_t k = e / S, t = e - k * S;
         float2 o = out[e];
-        o.x += C[k * cols_pad + t];
-        o.y += C[(K + k) * cols_pad + t];
+        o.x = (float)((double)o.x + seg_sum(C, nseg, seg_stride, k * cols_pad + t));
+        o.y = (float)((double)o.y + seg_sum(C, nseg, seg_stride, (K + k) * cols_pad + t));
         out[e] = o;
     }
 }
 
 // weighted: W[p][t] = (C[p][t], C[P+p][t])
-__global__ void k_finish_weighted(const float *__restrict__ C, int64_t cols_pad, int64_t P, int64_t S,
-                                  float2 *__restrict__ W)
+__global__ void k_finish_weighted(const float *__restrict__ C, int64_t nseg, int64_t seg_stride, int64_t cols_pad,
+                                  int64_t P, int64_t S, float2 *__restrict__ W)
 {
     const int64_t total = P * S;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
     {
         const int64_t p = e / S, t = e - p * S;
-        W[e] = make_float2(C[p * cols_pad + t], C[(P + p) * cols_pad + t]);
+        W[e] = make_float2((float)seg_sum(C, nseg, seg_stride, p * cols_pad + t),
+                           (float)seg_sum(C, nseg, seg_stride, (P + p) * cols_pad + t));
     }
 }
 
@@ -383,28 +402,50 @@ unsigned grid_for(int64_t n)
     return (unsigned)(b < 1 ? 1 : (b > 152 * 16 ? 152 * 16 : b));
 }
 
+// 32-deep chunks per float32 accumulation segment: one chunk (12 MMAs of
+// K=8) per segment keeps the tensor core's float32 accumulation short.
+constexpr int64_t SEG_CHUNKS = 1;
+
+struct GemmLayout
+{
+    int64_t Mp, Np, Kp, kchunks, nseg;
+    float *a_hi, *a_lo, *b_hi, *b_lo, *C;
+};
+
+GemmLayout layout(int64_t M, int64_t N, int64_t Kd, void *ws)
+{
+    GemmLayout g{};
+    g.Mp = round_up(M, TM);
+    g.Np = round_up(N, TN);
+    g.Kp = round_up(Kd, TK);
+    g.kchunks = g.Kp / TK;
+    g.nseg = (g.kchunks + SEG_CHUNKS - 1) / SEG_CHUNKS;
+    float *p = (float *)(((uintptr_t)ws + 255) & ~(uintptr_t)255);
+    g.a_hi = p;
+    g.a_lo = g.a_hi + g.Mp * g.Kp;
+    g.b_hi = g.a_lo + g.Mp * g.Kp;
+    g.b_lo = g.b_hi + g.Np * g.Kp;
+    g.C = g.b_lo + g.Np * g.Kp;
+    return g;
+}
+
+cudaError_t run_gemm(const GemmLayout &g, cudaStream_t st)
+{
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(k_gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES)))
+        return e;
+    dim3 grid((unsigned)(g.Np / TN), (unsigned)(g.Mp / TM), (unsigned)g.nseg);
+    k_gemm_tf32x3<<<grid, 128, SMEM_BYTES, st>>>(g.a_hi, g.a_lo, g.b_hi, g.b_lo, g.kchunks, SEG_CHUNKS, g.Mp, g.Np,
+                                                 g.C);
+    return launched();
+}
+
 } // namespace
 
 size_t tc_workspace_bytes(int64_t M, int64_t N, int64_t Kd)
 {
-    const int64_t Mp = round_up(M, TM), Np = round_up(N, TN), Kp = round_up(Kd, TK);
-    return (size_t)(2 * Mp * Kp + 2 * Np * Kp + Mp * Np) * sizeof(float) + 256;
-}
-
-static cudaError_t run_gemm(int64_t M, int64_t N, int64_t Kd, void *ws, float **a_hi, float **a_lo, float **b_hi,
-                            float **b_lo, float **C, int64_t *Mp_out, int64_t *Np_out, int64_t *Kp_out)
-{
-    const int64_t Mp = round_up(M, TM), Np = round_up(N, TN), Kp = round_up(Kd, TK);
-    float *p = (float *)(((uintptr_t)ws + 255) & ~(uintptr_t)255);
-    *a_hi = p;
-    *a_lo = *a_hi + Mp * Kp;
-    *b_hi = *a_lo + Mp * Kp;
-    *b_lo = *b_hi + Np * Kp;
-    *C = *b_lo + Np * Kp;
-    *Mp_out = Mp;
-    *Np_out = Np;
-    *Kp_out = Kp;
-    return cudaSuccess;
+    const GemmLayout g = layout(M, N, Kd, nullptr);
+    return (size_t)(2 * g.Mp * g.Kp + 2 * g.Np * g.Kp + g.nseg * g.Mp * g.Np) * sizeof(float) + 256;
 }
 
 cudaError_t launch_contract_tc_expect(const void *H, const double *E, int64_t P, int64_t K, int64_t S, void *out,
@@ -412,23 +453,17 @@ cudaError_t launch_contract_tc_expect(const void *H, const double *E, int64_t P,
 {
     if (K <= 0 || S <= 0 || P <= 0)
         return cudaSuccess;
-    float *ah, *al, *bh, *bl, *C;
-    int64_t Mp, Np, Kp;
-    run_gemm(2 * K, S, P, ws, &ah, &al, &bh, &bl, &C, &Mp, &Np, &Kp);
+    const GemmLayout g = layout(2 * K, S, P, ws);
     cudaError_t e;
-    k_prep_a_expect<<<grid_for(Mp * Kp), 256, 0, st>>>((const float2 *)H, P, K, Mp, Kp, ah, al);
+    k_prep_a_expect<<<grid_for(g.Mp * g.Kp), 256, 0, st>>>((const float2 *)H, P, K, g.Mp, g.Kp, g.a_hi, g.a_lo);
     if ((e = launched()))
         return e;
-    k_prep_b_expect<<<grid_for(Np * Kp), 256, 0, st>>>(E, P, S, Np, Kp, bh, bl);
+    k_prep_b_expect<<<grid_for(g.Np * g.Kp), 256, 0, st>>>(E, P, S, g.Np, g.Kp, g.b_hi, g.b_lo);
     if ((e = launched()))
         return e;
-    if ((e = cudaFuncSetAttribute(k_gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES)))
+    if ((e = run_gemm(g, st)))
         return e;
-    dim3 grid((unsigned)(Np / TN), (unsigned)(Mp / TM));
-    k_gemm_tf32x3<<<grid, 128, SMEM_BYTES, st>>>(ah, al, bh, bl, Kp / TK, Np, C);
-    if ((e = launched()))
-        return e;
-    k_finish_expect<<<grid_for(K * S), 256, 0, st>>>(C, Np, K, S, (float2 *)out);
+    k_finish_expect<<<grid_for(K * S), 256, 0, st>>>(g.C, g.nseg, g.Mp * g.Np, g.Np, K, S, (float2 *)out);
     return launched();
 }
 
@@ -437,23 +472,17 @@ cudaError_t launch_weighted_tc(const void *H, const float *X, int64_t P, int64_t
 {
     if (P <= 0 || S <= 0)
         return cudaSuccess;
-    float *ah, *al, *bh, *bl, *C;
-    int64_t Mp, Np, Kp;
-    run_gemm(2 * P, S, K, ws, &ah, &al, &bh, &bl, &C, &Mp, &Np, &Kp);
+    const GemmLayout g = layout(2 * P, S, K, ws);
     cudaError_t e;
-    k_prep_a_weighted<<<grid_for(Mp * Kp), 256, 0, st>>>((const float2 *)H, P, K, Mp, Kp, ah, al);
+    k_prep_a_weighted<<<grid_for(g.Mp * g.Kp), 256, 0, st>>>((const float2 *)H, P, K, g.Mp, g.Kp, g.a_hi, g.a_lo);
     if ((e = launched()))
         return e;
-    k_prep_b_weighted<<<grid_for(Np * Kp), 256, 0, st>>>(X, K, S, Np, Kp, bh, bl);
+    k_prep_b_weighted<<<grid_for(g.Np * g.Kp), 256, 0, st>>>(X, K, S, g.Np, g.Kp, g.b_hi, g.b_lo);
     if ((e = launched()))
         return e;
-    if ((e = cudaFuncSetAttribute(k_gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES)))
+    if ((e = run_gemm(g, st)))
         return e;
-    dim3 grid((unsigned)(Np / TN), (unsigned)(Mp / TM));
-    k_gemm_tf32x3<<<grid, 128, SMEM_BYTES, st>>>(ah, al, bh, bl, Kp / TK, Np, C);
-    if ((e = launched()))
-        return e;
-    k_finish_weighted<<<grid_for(P * S), 256, 0, st>>>(C, Np, P, S, (float2 *)W);
+    k_finish_weighted<<<grid_for(P * S), 256, 0, st>>>(g.C, g.nseg, g.Mp * g.Np, g.Np, P, S, (float2 *)W);
     return launched();
 }
 

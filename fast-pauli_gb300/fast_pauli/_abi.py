@@ -101,11 +101,11 @@ SIGNATURES.update({
 
 class BatchTuning(ctypes.Structure):
     _fields_ = [("threads_per_cta", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
-                ("rows_per_item", ctypes.c_int32)]
+                ("rows_per_item", ctypes.c_int32), ("tile_mb", ctypes.c_int32)]
 
     def as_dict(self) -> dict:
         return {"threads_per_cta": self.threads_per_cta, "ctas_per_sm": self.ctas_per_sm,
-                "rows_per_item": self.rows_per_item}
+                "rows_per_item": self.rows_per_item, "tile_mb": self.tile_mb}
 
 
 class FpgError(RuntimeError):

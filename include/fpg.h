@@ -174,6 +174,7 @@ typedef struct fpg_batch_tuning
     int32_t threads_per_cta; /* 128 or 256                                          */
     int32_t ctas_per_sm;     /* CTAs per SM of each persistent grid, 1..8          */
     int32_t rows_per_item;   /* rows of one work item, power of two >= 32          */
+    int32_t tile_mb;         /* column-tile budget (MiB) for L2 residency, >= 1   */
 } fpg_batch_tuning;
 
 int fpg_batch_create(int32_t dtype, fpg_batch **out);

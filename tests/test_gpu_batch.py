@@ -117,7 +117,7 @@ def test_batch_argument_errors():
     assert L.fpg_batch_add(b.handle, op.handle, buf.data_ptr(), 0, buf.data_ptr(), buf.data_ptr(), 1) == \
         _abi.FPG_ERR_INVALID
     assert L.fpg_batch_plan(b.handle, None) == _abi.FPG_ERR_INVALID  # empty batch
-    bad = _abi.BatchTuning(96, 4, 4096)
+    bad = _abi.BatchTuning(96, 4, 4096, 40)
     b.add(op, buf.data_ptr(), 1, buf.data_ptr(), buf.data_ptr(), 1)
     assert L.fpg_batch_plan(b.handle, ctypes.byref(bad)) == _abi.FPG_ERR_INVALID
     assert L.fpg_batch_create(9, ctypes.byref(ctypes.c_void_p())) == _abi.FPG_ERR_INVALID
