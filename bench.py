@@ -320,6 +320,40 @@ def cpu_sample(strings, h, psi, S, n):
             "sample": f"first {sub} of 861 strings, K=1000, all 16384x1024 states ({t:.2f} s)"}
 
 
+def run_profile_c64(args):
+    """One-shot complex64 cases for ncu captures (warm-up + args.steps calls)."""
+    import numpy as np
+    import torch
+
+    import oracle
+    from fast_pauli import _abi
+
+    torch.cuda.set_device(0)
+    if args.profile == "mixed":
+        n, K, S = 18, 1000, 512
+        strings, h, psi = config2(n=n, K=K, S=S, seed=1003)
+    else:
+        n, K, S = 20, 1, 64
+        rng = np.random.default_rng(1006)
+        strings = oracle.uniform_strings(rng, n, 1024)
+        h = rng.standard_normal((len(strings), K)) + 1j * rng.standard_normal((len(strings), K))
+        g = torch.Generator(device="cuda").manual_seed(6)
+        psi = torch.complex(torch.randn(1 << n, S, dtype=torch.float64, device="cuda", generator=g),
+                            torch.randn(1 << n, S, dtype=torch.float64, device="cuda", generator=g))
+        psi /= torch.linalg.vector_norm(psi, dim=0, keepdim=True)
+    L = _abi.lib()
+    op = _abi.Operator(strings)
+    stream = _stream_handle()
+    h64 = torch.from_numpy(h).to(torch.complex64).cuda()
+    psi64 = psi.to(torch.complex64)
+    del psi
+    out = torch.zeros((K, S), dtype=torch.complex64, device="cuda")
+    for _ in range(max(1, args.warmup) + args.steps):
+        _abi.check(L.fpg_summed_expect(op.handle, h64.data_ptr(), K, psi64.data_ptr(), out.data_ptr(), S,
+                                       _abi.FPG_C64, stream))
+    torch.cuda.synchronize()
+
+
 def run_mixed(args):
     """complex64 / float32 path on the n=18 shape; error vs the float64 GPU path."""
     import numpy as np
@@ -609,7 +643,10 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--profile", action="store_true", help="short device-only run for ncu captures")
+    ap.add_argument("--profile", nargs="?", const="summed", default=None, choices=["summed", "mixed", "random"],
+                    help="short device-only run for ncu captures: summed = configuration 2 (float64), "
+                         "mixed = the n=18 complex64 shape (tensor-core contraction), "
+                         "random = n=20, 1024 uniform random strings, 64 states, complex64")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-mixed", action="store_true")
@@ -625,6 +662,9 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     dist = None
+    if args.profile in ("mixed", "random"):
+        run_profile_c64(args)
+        return
     if args.workload != "summed" and args.impl == "ours":
         if rank == 0:
             line = run_batch(args) if args.workload == "batch" else run_serve(args)

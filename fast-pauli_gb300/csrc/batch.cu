@@ -6,9 +6,11 @@
 // e.g. 256 PauliOp.expectation_value calls (reference __pauli_op.hpp:482-549)
 // that would otherwise be 256 separate calls.  Planning turns every problem
 // into work items (entry, chunk, column tile, row split) of the expectation
-// kernel; one persistent kernel per chunk class (at most 8, usually 1-3)
-// pulls items from a device work queue (atomic counter), so small problems
-// fill the gaps left by large ones and no launch is wasted on a tail.  Item
+// kernel; one persistent kernel per (chunk class, vector width) bucket pulls
+// items from a device work queue (atomic counter), so small problems fill the
+// gaps left by large ones and no launch is wasted on a tail (tuning
+// ctas_per_sm = -1 instead launches one CTA per item and lets the hardware
+// block scheduler drain them; the autotuner picks).  Item
 // order: problems largest first, then column tile, row split, chunk (chunks
 // fastest, so concurrently running CTAs share rows in L2).  Partial sums go
 // to per-problem (split, string, state) tables, reduced in place in a fixed
@@ -50,8 +52,10 @@ struct BatchEntry
     int32_t n;
     int32_t TC;
     int32_t n_splits;
-    int32_t pad;
+    int32_t V; // complex elements per lane (2 only for complex64 with an even state count)
 };
+
+constexpr int kBuckets = 2 * kNumChunkClasses; // (chunk class, V in {1, 2})
 
 struct BatchItem
 {
@@ -64,12 +68,18 @@ struct BatchItem
 namespace
 {
 
-template <typename T, int GE, int GO>
-__global__ void __launch_bounds__(256) k_batch_expect(const BatchEntry *__restrict__ entries,
+// float32 chunks of up to four strings do little arithmetic per row and are
+// bound by memory latency: ask the compiler for three resident 256-thread CTAs
+// per SM (<= 85 registers), as the per-call kernel does.  Larger chunks and
+// float64 keep the default.
+template <typename T, int G> constexpr int kBatchMinBlocks = (sizeof(T) == 4 && G <= 4) ? 3 : 1;
+
+template <typename T, int V, int GE, int GO>
+__global__ void __launch_bounds__(256, kBatchMinBlocks<T, GE + GO>) k_batch_expect(const BatchEntry *__restrict__ entries,
                                                       const BatchItem *__restrict__ items, int n_items,
                                                       int *__restrict__ counter)
 {
-    extern __shared__ double red[]; // blockDim.x doubles
+    extern __shared__ double red[]; // blockDim.x * V doubles
     __shared__ int s_item;
     for (;;)
     {
@@ -82,9 +92,23 @@ __global__ void __launch_bounds__(256) k_batch_expect(const BatchEntry *__restri
             break;
         const BatchItem bi = items[it];
         const BatchEntry &e = entries[bi.entry];
-        expect_chunk_body<T, 1, GE, GO>((const T *)e.psi, e.S, e.n, e.recs, e.orig, e.P, e.chunks[bi.chunk], e.TC,
+        expect_chunk_body<T, V, GE, GO>((const T *)e.psi, e.S, e.n, e.recs, e.orig, e.P, e.chunks[bi.chunk], e.TC,
                                         (int64_t)bi.ctile, bi.split, e.n_splits, e.partial, red);
     }
+}
+
+// Item-grid form: one CTA per work item (blockIdx.x); the hardware block
+// scheduler hands out items as SMs free up.  Same work as the persistent form
+// without its loop-carried state.
+template <typename T, int V, int GE, int GO>
+__global__ void __launch_bounds__(256, kBatchMinBlocks<T, GE + GO>) k_batch_items(const BatchEntry *__restrict__ entries,
+                                                     const BatchItem *__restrict__ items)
+{
+    extern __shared__ double red[]; // blockDim.x * V doubles
+    const BatchItem bi = items[blockIdx.x];
+    const BatchEntry &e = entries[bi.entry];
+    expect_chunk_body<T, V, GE, GO>((const T *)e.psi, e.S, e.n, e.recs, e.orig, e.P, e.chunks[bi.chunk], e.TC,
+                                    (int64_t)bi.ctile, bi.split, e.n_splits, e.partial, red);
 }
 
 __device__ __forceinline__ int find_entry(const BatchEntry *entries, int n_entries, int64_t idx, bool contraction)
@@ -162,14 +186,14 @@ struct fpg_batch
         int64_t S;
     };
     std::vector<Problem> problems;
-    fpg_batch_tuning tuning{256, 4, 1 << 12, 40};
+    fpg_batch_tuning tuning{256, 0, 1 << 15, 40};
     bool planned = false;
     // device state of the plan
     BatchEntry *d_entries = nullptr;
     BatchItem *d_items = nullptr;
     int *d_counters = nullptr;
     double *d_partial = nullptr;
-    int class_begin[kNumChunkClasses + 1] = {};
+    int bucket_begin[kBuckets + 1] = {}; // items of bucket (class, V) contiguous
     int64_t red_total = 0, con_total = 0;
     int grid = 0;
     cudaGraphExec_t exec = nullptr;
@@ -206,14 +230,18 @@ int tc_for(int64_t S)
     return tc;
 }
 
-template <typename T>
-cudaError_t launch_class(int cls, int grid, int threads, const BatchEntry *e, const BatchItem *items, int n_items,
-                         int *counter, cudaStream_t st)
+template <typename T, int V>
+cudaError_t launch_class_v(int cls, int grid, int threads, const BatchEntry *e, const BatchItem *items, int n_items,
+                           int *counter, cudaStream_t st)
 {
-    const size_t smem = (size_t)threads * sizeof(double);
+    const size_t smem = (size_t)threads * V * sizeof(double);
+    // grid < 0: item-grid form (one CTA per item)
 #define FPG_BCASE(ID, GE, GO)                                                                                          \
     case ID:                                                                                                           \
-        k_batch_expect<T, GE, GO><<<grid, threads, smem, st>>>(e, items, n_items, counter);                           \
+        if (grid < 0)                                                                                                  \
+            k_batch_items<T, V, GE, GO><<<(unsigned)n_items, threads, smem, st>>>(e, items);                           \
+        else                                                                                                           \
+            k_batch_expect<T, V, GE, GO><<<grid, threads, smem, st>>>(e, items, n_items, counter);                    \
         break;
     switch (cls)
     {
@@ -232,15 +260,14 @@ cudaError_t launch_class(int cls, int grid, int threads, const BatchEntry *e, co
     return launched();
 }
 
-int max_resident(int cls, bool fp32, int threads)
+template <typename T, int V> int max_resident_v(int cls, int threads)
 {
     int nb = 0;
-    const size_t smem = (size_t)threads * sizeof(double);
-    cudaError_t e = cudaSuccess;
+    const size_t smem = (size_t)threads * V * sizeof(double);
+    cudaError_t e = cudaErrorInvalidValue;
 #define FPG_OCC(ID, GE, GO)                                                                                            \
     case ID:                                                                                                           \
-        e = fp32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_expect<float, GE, GO>, threads, smem)    \
-                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_expect<double, GE, GO>, threads, smem);  \
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_expect<T, V, GE, GO>, threads, smem);           \
         break;
     switch (cls)
     {
@@ -264,17 +291,39 @@ int max_resident(int cls, bool fp32, int threads)
     return nb < 1 ? 1 : nb;
 }
 
+// bucket = 2 * class + (V - 1); V = 2 exists for complex64 only
+cudaError_t launch_bucket(bool fp32, int bucket, int grid, int threads, const BatchEntry *e, const BatchItem *items,
+                          int n_items, int *counter, cudaStream_t st)
+{
+    const int cls = bucket / 2, V = bucket % 2 + 1;
+    if (!fp32)
+        return V == 1 ? launch_class_v<double, 1>(cls, grid, threads, e, items, n_items, counter, st)
+                      : cudaErrorInvalidValue;
+    return V == 1 ? launch_class_v<float, 1>(cls, grid, threads, e, items, n_items, counter, st)
+                  : launch_class_v<float, 2>(cls, grid, threads, e, items, n_items, counter, st);
+}
+
+int max_resident(bool fp32, int bucket, int threads)
+{
+    const int cls = bucket / 2, V = bucket % 2 + 1;
+    if (!fp32)
+        return max_resident_v<double, 1>(cls, threads);
+    return V == 1 ? max_resident_v<float, 1>(cls, threads) : max_resident_v<float, 2>(cls, threads);
+}
+
 int do_plan(fpg_batch *b, const fpg_batch_tuning &t)
 {
     if (t.threads_per_cta != 128 && t.threads_per_cta != 256)
         return set_error(FPG_ERR_INVALID, "threads_per_cta must be 128 or 256");
-    if (t.ctas_per_sm < 1 || t.ctas_per_sm > 8)
-        return set_error(FPG_ERR_INVALID, "ctas_per_sm must be in [1, 8]");
+    if (t.ctas_per_sm < -1 || t.ctas_per_sm > 8)
+        return set_error(FPG_ERR_INVALID,
+                         "ctas_per_sm must be in [-1, 8] (0: as many as fit; -1: one CTA per work item)");
     if (t.rows_per_item < 32 || (t.rows_per_item & (t.rows_per_item - 1)))
         return set_error(FPG_ERR_INVALID, "rows_per_item must be a power of two >= 32");
     if (t.tile_mb < 1)
         return set_error(FPG_ERR_INVALID, "tile_mb must be >= 1");
     b->free_plan();
+    const bool fp32 = b->dtype == FPG_C64;
     const int np = (int)b->problems.size();
     // largest problems first
     std::vector<int> order((size_t)np);
@@ -287,8 +336,8 @@ int do_plan(fpg_batch *b, const fpg_batch_tuning &t)
         return wa > wc;
     });
     std::vector<BatchEntry> entries((size_t)np);
-    std::vector<std::vector<BatchItem>> by_class(kNumChunkClasses);
-    int64_t partial_total = 0, red_off = 0, con_off = 0;
+    std::vector<std::vector<BatchItem>> by_bucket(kBuckets);
+    const int64_t tile_budget = (int64_t)t.tile_mb << 20;
     for (int pos = 0; pos < np; ++pos)
     {
         const int i = order[(size_t)pos];
@@ -305,32 +354,50 @@ int do_plan(fpg_batch *b, const fpg_batch_tuning &t)
         e.P = op->P;
         e.K = p.K;
         e.n = op->n;
-        e.TC = column_lanes_for_l2(std::min(tc_for(p.S), t.threads_per_cta), op->n, b->dtype == FPG_C64 ? 8 : 16, (int64_t)t.tile_mb << 20);
+        // same tiling rules as a single call: vector width, L2-line-wide column
+        // tiles, and row windows (splits) only when a tile cannot stay in L2
+        e.V = (fp32 && p.S % 2 == 0 && ((uintptr_t)p.psi % 16) == 0) ? 2 : 1;
+        const int bpl = e.V * (fp32 ? 8 : 16);
+        e.TC = column_lanes_for_l2(std::min(tc_for((p.S + e.V - 1) / e.V), t.threads_per_cta), op->n, bpl,
+                                   tile_budget);
         const int64_t NB = op->n >= 5 ? ((int64_t)1 << (op->n - 5)) : 1;
-        const int64_t blocks_per_item = std::max<int64_t>(1, t.rows_per_item / 32);
-        e.n_splits = (int32_t)std::max<int64_t>(1, std::min<int64_t>(64, NB / blocks_per_item));
+        const int64_t window = std::max<int64_t>(1, t.rows_per_item / 32);
+        e.n_splits = 1;
+        if (column_tile_footprint(e.TC, op->n, bpl) > tile_budget)
+            e.n_splits = (int32_t)std::max<int64_t>(1, std::min<int64_t>(256, (NB / 2 + window - 1) / window));
+        const int64_t ctiles = (e.S + (int64_t)e.TC * e.V - 1) / ((int64_t)e.TC * e.V);
+        for (int c = 0; c < kNumChunkClasses; ++c)
+        {
+            auto &dst = by_bucket[(size_t)(2 * c + (e.V - 1))];
+            for (int64_t ct = 0; ct < ctiles; ++ct)
+                for (int s = 0; s < e.n_splits; ++s)
+                    for (int ch = op->class_begin[(size_t)c]; ch < op->class_begin[(size_t)c + 1]; ++ch)
+                        dst.push_back(BatchItem{i, ch, (int32_t)ct, s});
+        }
+    }
+    std::vector<BatchItem> items;
+    for (int k = 0; k < kBuckets; ++k)
+    {
+        b->bucket_begin[k] = (int)items.size();
+        items.insert(items.end(), by_bucket[(size_t)k].begin(), by_bucket[(size_t)k].end());
+    }
+    b->bucket_begin[kBuckets] = (int)items.size();
+    if (items.size() > (size_t)0x7fffffff)
+        return set_error(FPG_ERR_UNSUPPORTED, "batch has too many work items");
+    // entries keep the order of addition: partial tables and the flattened
+    // index spaces of reduction and contraction are laid out in that order
+    int64_t partial_total = 0, red_off = 0, con_off = 0;
+    for (int i = 0; i < np; ++i)
+    {
+        BatchEntry &e = entries[(size_t)i];
         e.red_off = red_off;
         e.con_off = con_off;
         red_off += e.P * e.S;
         con_off += e.K * e.S;
         partial_total += (int64_t)e.n_splits * e.P * e.S;
-        const int64_t ctiles = (e.S + e.TC - 1) / e.TC;
-        for (int c = 0; c < kNumChunkClasses; ++c)
-            for (int64_t ct = 0; ct < ctiles; ++ct)
-                for (int s = 0; s < e.n_splits; ++s)
-                    for (int ch = op->class_begin[(size_t)c]; ch < op->class_begin[(size_t)c + 1]; ++ch)
-                        by_class[(size_t)c].push_back(BatchItem{i, ch, (int32_t)ct, s});
     }
-    std::vector<BatchItem> items;
-    for (int c = 0; c < kNumChunkClasses; ++c)
-    {
-        b->class_begin[c] = (int)items.size();
-        items.insert(items.end(), by_class[(size_t)c].begin(), by_class[(size_t)c].end());
-    }
-    b->class_begin[kNumChunkClasses] = (int)items.size();
-    if (items.size() > (size_t)0x7fffffff)
-        return set_error(FPG_ERR_UNSUPPORTED, "batch has too many work items");
-    // device-side partial tables
+    b->red_total = red_off;
+    b->con_total = con_off;
     cudaError_t err = cudaSuccess;
     if ((err = cudaMalloc((void **)&b->d_partial, (size_t)std::max<int64_t>(1, partial_total) * sizeof(double))))
     {
@@ -338,38 +405,25 @@ int do_plan(fpg_batch *b, const fpg_batch_tuning &t)
         return cuda_error(err, "fpg_batch_plan: partial tables");
     }
     int64_t off = 0;
-    // entries keep the order of addition; offsets into the partial buffer by addition order
     for (int i = 0; i < np; ++i)
     {
         entries[(size_t)i].partial = b->d_partial + off;
         off += (int64_t)entries[(size_t)i].n_splits * entries[(size_t)i].P * entries[(size_t)i].S;
     }
-    // red/con offsets must be monotone in entry index for the binary search:
-    // recompute them in addition order
-    red_off = con_off = 0;
-    for (int i = 0; i < np; ++i)
-    {
-        entries[(size_t)i].red_off = red_off;
-        entries[(size_t)i].con_off = con_off;
-        red_off += entries[(size_t)i].P * entries[(size_t)i].S;
-        con_off += entries[(size_t)i].K * entries[(size_t)i].S;
-    }
-    b->red_total = red_off;
-    b->con_total = con_off;
     if ((err = cudaMalloc((void **)&b->d_entries, entries.size() * sizeof(BatchEntry))) ||
         (err = cudaMemcpy(b->d_entries, entries.data(), entries.size() * sizeof(BatchEntry),
                           cudaMemcpyHostToDevice)) ||
         (err = cudaMalloc((void **)&b->d_items, std::max<size_t>(1, items.size()) * sizeof(BatchItem))) ||
         (!items.empty() &&
          (err = cudaMemcpy(b->d_items, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice))) ||
-        (err = cudaMalloc((void **)&b->d_counters, kNumChunkClasses * sizeof(int))))
+        (err = cudaMalloc((void **)&b->d_counters, kBuckets * sizeof(int))))
     {
         b->free_plan();
         return cuda_error(err, "fpg_batch_plan: work queue");
     }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
-    b->grid = sms * t.ctas_per_sm;
+    b->grid = t.ctas_per_sm > 0 ? sms * t.ctas_per_sm : 1 << 30; // 0: capped by residency at launch
     b->tuning = t;
     b->planned = true;
     return FPG_OK;
@@ -379,22 +433,23 @@ int do_run(fpg_batch *b, cudaStream_t st)
 {
     const bool fp32 = b->dtype == FPG_C64;
     cudaError_t e;
-    if ((e = cudaMemsetAsync(b->d_counters, 0, kNumChunkClasses * sizeof(int), st)))
+    if ((e = cudaMemsetAsync(b->d_counters, 0, kBuckets * sizeof(int), st)))
         return cuda_error(e, "cudaMemsetAsync");
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
-    for (int c = 0; c < kNumChunkClasses; ++c)
+    for (int k = 0; k < kBuckets; ++k)
     {
-        const int n_items = b->class_begin[c + 1] - b->class_begin[c];
+        const int n_items = b->bucket_begin[k + 1] - b->bucket_begin[k];
         if (n_items <= 0)
             continue;
-        const int cap = sms * max_resident(c, fp32, b->tuning.threads_per_cta);
-        const int grid = std::max(1, std::min({b->grid, cap, n_items}));
-        e = fp32 ? launch_class<float>(c, grid, b->tuning.threads_per_cta, b->d_entries,
-                                       b->d_items + b->class_begin[c], n_items, b->d_counters + c, st)
-                 : launch_class<double>(c, grid, b->tuning.threads_per_cta, b->d_entries,
-                                        b->d_items + b->class_begin[c], n_items, b->d_counters + c, st);
-        if (e)
+        int grid = -1; // item-grid form
+        if (b->tuning.ctas_per_sm >= 0)
+        {
+            const int cap = sms * max_resident(fp32, k, b->tuning.threads_per_cta);
+            grid = std::max(1, std::min({b->grid, cap, n_items}));
+        }
+        if ((e = launch_bucket(fp32, k, grid, b->tuning.threads_per_cta, b->d_entries, b->d_items + b->bucket_begin[k],
+                               n_items, b->d_counters + k, st)))
             return cuda_error(e, "persistent batch kernel");
     }
     const int np = (int)b->problems.size();
@@ -531,8 +586,8 @@ extern "C"
         cudaStream_t st = (cudaStream_t)stream;
         // candidate grid: CTA size x residency x work-item granularity
         const int threads[] = {128, 256};
-        const int ctas[] = {4, 8};
-        const int rows[] = {1 << 11, 1 << 13};
+        const int ctas[] = {0, -1};
+        const int rows[] = {1 << 15, 1 << 17};
         const int tiles[] = {16, 48};
         fpg_batch_tuning top{};
         double top_ms = 1e300;
@@ -595,7 +650,7 @@ extern "C"
         if (n_problems)
             *n_problems = (int64_t)b->problems.size();
         if (n_items)
-            *n_items = b->planned ? b->class_begin[kNumChunkClasses] : 0;
+            *n_items = b->planned ? b->bucket_begin[kBuckets] : 0;
         if (tuning)
             *tuning = b->tuning;
         return FPG_OK;

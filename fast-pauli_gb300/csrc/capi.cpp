@@ -192,10 +192,62 @@ void free_dev(fpg_operator *op)
     cudaFree(op->d_orig);
     cudaFree(op->d_groups);
     cudaFree(op->d_chunks);
+    cudaFree(op->d_fast_chunks);
+    cudaFree(op->d_wht);
     op->d_recs = nullptr;
     op->d_orig = nullptr;
     op->d_groups = nullptr;
     op->d_chunks = nullptr;
+    op->d_fast_chunks = nullptr;
+    op->d_wht = nullptr;
+}
+
+// Per-call decomposition: large x-groups -> transform-kernel chunks, the
+// rest -> direct-kernel chunks bucketed by class.
+void build_fast_decomposition(fpg_operator *op)
+{
+    op->wht.clear();
+    op->wht_max_count = 0;
+    std::vector<std::vector<Chunk>> by_class(kNumChunkClasses);
+    std::vector<char> is_wht(op->groups.size(), 0);
+    for (size_t gi = 0; gi < op->groups.size(); ++gi)
+    {
+        const Group &g = op->groups[gi];
+        if (g.count < kWhtMinStrings)
+            continue;
+        is_wht[gi] = 1;
+        int32_t n_even_total = 0;
+        while (n_even_total < g.count && (op->recs[(size_t)(g.begin + n_even_total)].meta & 1u) == 0)
+            ++n_even_total;
+        for (int32_t b = 0; b < g.count; b += kWhtMaxStrings)
+        {
+            const int32_t cnt = std::min<int32_t>(kWhtMaxStrings, g.count - b);
+            const int32_t ne = std::max<int32_t>(0, std::min<int32_t>(cnt, n_even_total - b));
+            op->wht.push_back(WhtChunk{g.x, g.begin + b, (int16_t)cnt, (int16_t)ne});
+            op->wht_max_count = std::max(op->wht_max_count, (int)cnt);
+        }
+    }
+    // direct chunks of the remaining groups, in the order of the full decomposition
+    for (int c = 0; c < kNumChunkClasses; ++c)
+        for (int i = op->class_begin[(size_t)c]; i < op->class_begin[(size_t)c + 1]; ++i)
+        {
+            const Chunk &ch = op->chunks[(size_t)i];
+            // the chunk's group: the one containing its first string
+            const int32_t first = ch.n_even > 0 ? ch.begin_even : ch.begin_odd;
+            const auto it = std::upper_bound(op->groups.begin(), op->groups.end(), first,
+                                             [](int32_t v, const Group &g) { return v < g.begin; });
+            const size_t gi = (size_t)(it - op->groups.begin()) - 1;
+            if (!is_wht[gi])
+                by_class[(size_t)c].push_back(ch);
+        }
+    op->fast_chunks.clear();
+    op->fast_class_begin.assign(kNumChunkClasses + 1, 0);
+    for (int c = 0; c < kNumChunkClasses; ++c)
+    {
+        op->fast_class_begin[(size_t)c] = (int)op->fast_chunks.size();
+        op->fast_chunks.insert(op->fast_chunks.end(), by_class[(size_t)c].begin(), by_class[(size_t)c].end());
+    }
+    op->fast_class_begin[kNumChunkClasses] = (int)op->fast_chunks.size();
 }
 
 int check_dtype(int32_t dtype)
@@ -251,11 +303,16 @@ ExpectPlan plan_expect(const fpg_operator *op, int64_t S, bool fp32, const void 
     p.TC = column_lanes_for_l2(pick_tc(lanes), op->n, p.V * (fp32 ? 8 : 16), kColumnTileBytes);
     p.n_ctiles = (int)((S + (int64_t)p.TC * p.V - 1) / ((int64_t)p.TC * p.V));
     const int TR = 256 / p.TC;
-    const int64_t n_chunks = (int64_t)op->chunks.size();
-    const int64_t ctas = n_chunks * p.n_ctiles;
+    p.wht_TC = column_lanes_for_l2(pick_tc(S), op->n, fp32 ? 8 : 16, kColumnTileBytes);
+    p.wht_ctiles = (int)((S + p.wht_TC - 1) / p.wht_TC);
+    const int64_t ctas =
+        (int64_t)op->fast_chunks.size() * p.n_ctiles + (int64_t)op->wht.size() * p.wht_ctiles;
     const int64_t NB = op->n >= 5 ? ((int64_t)1 << (op->n - 5)) : 1;
     const int64_t target = 152 * 8; // CTAs in flight: ~8 resident per SM
     int64_t splits = (target + ctas - 1) / std::max<int64_t>(ctas, 1);
+    const int bpl = p.V * (fp32 ? 8 : 16);
+    if (column_tile_footprint(p.TC, op->n, bpl) > kColumnTileBytes)
+        splits = std::max<int64_t>(splits, (NB / 2 + kWindowBlocks - 1) / kWindowBlocks); // L2 row window
     const int64_t max_splits = std::max<int64_t>(1, NB / (2 * (int64_t)TR * 4)); // >= 4 blocks per row lane
     splits = std::max<int64_t>(1, std::min(splits, max_splits));
     splits = std::min<int64_t>(splits, 65535);
@@ -276,11 +333,15 @@ int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int6
         FPG_CUDA(partial.alloc((size_t)plan.n_splits * (size_t)op->P * (size_t)S * sizeof(double)));
         dst = (double *)partial.p;
     }
+    if (!op->wht.empty())
+        FPG_CUDA(launch_expect_wht(fp32, psi, S, op->n, dop, op->d_wht, (int)op->wht.size(), op->wht_max_count,
+                                   plan.wht_TC, plan.wht_ctiles, plan.n_splits, dst, st));
     for (int c = 0; c < kNumChunkClasses; ++c)
     {
-        const int b = op->class_begin[(size_t)c], e = op->class_begin[(size_t)c + 1];
+        const int b = op->fast_class_begin[(size_t)c], e = op->fast_class_begin[(size_t)c + 1];
         if (e > b)
-            FPG_CUDA(launch_expect_chunks(fp32, psi, S, op->n, dop, op->d_chunks + b, e - b, c, plan, dst, st));
+            FPG_CUDA(
+                launch_expect_chunks(fp32, psi, S, op->n, dop, op->d_fast_chunks + b, e - b, c, plan, dst, st));
     }
     if (plan.n_splits > 1)
         FPG_CUDA(launch_reduce_splits(dst, plan.n_splits, op->P * S, ev, st));
@@ -414,6 +475,11 @@ extern "C"
             e = upload(&op->d_groups, op->groups);
         if (e == cudaSuccess)
             e = upload(&op->d_chunks, op->chunks);
+        build_fast_decomposition(op);
+        if (e == cudaSuccess)
+            e = upload(&op->d_fast_chunks, op->fast_chunks);
+        if (e == cudaSuccess)
+            e = upload(&op->d_wht, op->wht);
         if (e != cudaSuccess)
         {
             free_dev(op);
@@ -453,18 +519,28 @@ extern "C"
     {
         if (!op)
             return set_error(FPG_ERR_INVALID, "op is null");
+        // the per-call decomposition: direct chunks + transform chunks
         const int64_t D = (int64_t)1 << op->n;
         int64_t visits = 0, adds = 0;
         for (int c = 0; c < kNumChunkClasses; ++c)
-            for (int i = op->class_begin[(size_t)c]; i < op->class_begin[(size_t)c + 1]; ++i)
+            for (int i = op->fast_class_begin[(size_t)c]; i < op->fast_class_begin[(size_t)c + 1]; ++i)
             {
-                const bool paired = (op->chunks[(size_t)i].x >> 5) != 0;
+                const bool paired = (op->fast_chunks[(size_t)i].x >> 5) != 0;
                 const int64_t rows = paired ? D / 2 : D;
                 visits += rows;
                 adds += rows * (kChunkClasses[c].ge + kChunkClasses[c].go);
             }
+        for (const WhtChunk &w : op->wht)
+        {
+            const bool paired = (w.x >> 4) != 0;
+            const int64_t rows = paired ? D / 2 : D;
+            const int parts = (w.n_even > 0 ? 1 : 0) + (w.n_even < w.count ? 1 : 0);
+            visits += rows;
+            // 16-point transform: 4 adds per row per part; one add per string per 16 rows
+            adds += rows * 4 * parts + (rows / 16) * w.count;
+        }
         if (n_chunks)
-            *n_chunks = (int64_t)op->chunks.size();
+            *n_chunks = (int64_t)(op->fast_chunks.size() + op->wht.size());
         if (row_visits)
             *row_visits = visits;
         if (sign_adds)

@@ -50,6 +50,20 @@ struct Group
     int32_t count;
 };
 
+// Work unit of the transform kernel (k_expect_wht.cu): `count` consecutive
+// sorted strings of one x-group starting at `begin`, the first n_even with
+// even #Y.  Groups with at least kWhtMinStrings strings use it, in pieces of
+// at most kWhtMaxStrings.
+struct WhtChunk
+{
+    uint64_t x;
+    int32_t begin;
+    int16_t count;
+    int16_t n_even;
+};
+constexpr int kWhtMinStrings = 10;
+constexpr int kWhtMaxStrings = 128;
+
 // Device-side view of an encoded operator.
 struct DevOp
 {
@@ -80,17 +94,28 @@ int chunk_class_for(int n_even, int n_odd); // smallest class covering, -1 if no
 // Column tiling for L2 residency.  All chunks of a launch sweep the same
 // column tile (2^n rows x TC lanes x bytes per lane) before moving to the
 // next, so the state is read from DRAM about once per launch when the tile
-// fits comfortably in the 126 MB L2; the partner rows (i ^ x) of random
-// strings then hit L2 too.  Narrow the tile (halve TC) until it fits the
-// budget, keeping at least 32 bytes per row access (one sector).
+// fits in the 126 MB L2.  L2 holds whole 128-byte lines, so a tile narrower
+// than 128 bytes per row costs as much L2 as a 128-byte one: narrow the tile
+// (halve TC) until it fits the budget, but not below one line per row.
 constexpr int64_t kColumnTileBytes = int64_t(40) << 20;
+constexpr int kL2Line = 128;
 inline int column_lanes_for_l2(int tc, int n, int bytes_per_lane, int64_t budget)
 {
-    const int min_tc = bytes_per_lane >= 32 ? 1 : 32 / bytes_per_lane;
+    const int min_tc = bytes_per_lane >= kL2Line ? 1 : kL2Line / bytes_per_lane;
     while (tc > min_tc && (int64_t(1) << n) * (int64_t)tc * bytes_per_lane > budget)
         tc >>= 1;
     return tc;
 }
+// L2 footprint of a column tile (whole lines).
+inline int64_t column_tile_footprint(int tc, int n, int bytes_per_lane)
+{
+    const int64_t w = (int64_t)tc * bytes_per_lane;
+    return (int64_t(1) << n) * (w < kL2Line ? kL2Line : w);
+}
+// When even a one-line tile does not fit, the row range is split so that the
+// CTAs running at the same time (chunks fastest, then splits) read rows from
+// a window of at most this many 32-row blocks, which L2 can hold.
+constexpr int64_t kWindowBlocks = 1024;
 
 struct ExpectPlan
 {
@@ -98,6 +123,8 @@ struct ExpectPlan
     int V;            // complex elements per lane (1 or 2)
     int n_ctiles;     // column tiles
     int n_splits;     // row splits (>1 -> partial buffer + reduction)
+    int wht_TC;       // column lanes of the transform kernel (V = 1)
+    int wht_ctiles;   // its column tiles
 };
 
 // ev_or_partial: [n_splits][P][S] float64 (row-major).  One launch per class.
@@ -105,6 +132,12 @@ cudaError_t launch_expect_chunks(bool fp32, const void *psi, int64_t S, int n, c
                                  int n_chunks, int cls, const ExpectPlan &plan, double *ev_or_partial,
                                  cudaStream_t st);
 cudaError_t launch_reduce_splits(const double *partial, int n_splits, int64_t count, double *ev, cudaStream_t st);
+
+// Transform kernel over WHT chunks (128 threads = TC column lanes x 128/TC row
+// lanes, one complex element per lane); writes like launch_expect_chunks.
+cudaError_t launch_expect_wht(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const WhtChunk *d_chunks,
+                              int n_chunks, int max_count, int TC, int n_ctiles, int n_splits, double *out,
+                              cudaStream_t st);
 
 // out(K,S) += H^T(K,P) * E(P,S); H complex (P,K), E real float64 (P,S).
 // out complex128 (fp32=false) or complex64 (fp32=true).

@@ -134,31 +134,50 @@ __device__ __forceinline__ void expect_chunk_body(const T *__restrict__ psi, int
                     bs[k][v] = T(0);
 
             const T *pa0 = psi + 2 * ((int64_t)base * S + t0);
+            // rows in groups of RG: all loads of a group are issued before any
+            // is consumed.  Single-string float32 chunks (random strings) have
+            // almost no arithmetic per row and batch 4 rows of loads; every
+            // other class keeps its registers for occupancy (measured: deeper
+            // batches cost the weight-2 float32 classes a CTA per SM).
+            constexpr int RG = (sizeof(T) == 4 && G == 1) ? 4 : 1;
 #pragma unroll
-            for (int r = 0; r < 32; ++r)
+            for (int r0 = 0; r0 < 32; r0 += RG)
             {
-                if (r < RB)
+                T ar[RG][V], ai[RG][V], br[RG][V], bi[RG][V];
+#pragma unroll
+                for (int g = 0; g < RG; ++g)
                 {
-                    T ar[V], ai[V], br[V], bi[V];
-                    load_cvec<T, V>(pa0 + 2 * (int64_t)r * S, ar, ai);
-                    load_cvec<T, V>(psi + 2 * ((int64_t)(baseB + (uint64_t)(r ^ xl)) * S + t0), br, bi);
-                    T qr[V], qi[V];
-#pragma unroll
-                    for (int v = 0; v < V; ++v)
+                    const int r = r0 + g;
+                    if (r < RB)
                     {
-                        qr[v] = fma(ar[v], br[v], ai[v] * bi[v]);
-                        qi[v] = fma(ar[v], bi[v], -(ai[v] * br[v]));
+                        load_cvec<T, V>(pa0 + 2 * (int64_t)r * S, ar[g], ai[g]);
+                        load_cvec<T, V>(psi + 2 * ((int64_t)(baseB + (uint64_t)(r ^ xl)) * S + t0), br[g], bi[g]);
                     }
+                }
 #pragma unroll
-                    for (int k = 0; k < GE; ++k)
+                for (int g = 0; g < RG; ++g)
+                {
+                    const int r = r0 + g;
+                    if (r < RB)
+                    {
+                        T qr[V], qi[V];
 #pragma unroll
                         for (int v = 0; v < V; ++v)
-                            bs[k][v] += flip_sign(qr[v], mk[k], r);
+                        {
+                            qr[v] = fma(ar[g][v], br[g][v], ai[g][v] * bi[g][v]);
+                            qi[v] = fma(ar[g][v], bi[g][v], -(ai[g][v] * br[g][v]));
+                        }
 #pragma unroll
-                    for (int k = 0; k < GO; ++k)
+                        for (int k = 0; k < GE; ++k)
 #pragma unroll
-                        for (int v = 0; v < V; ++v)
-                            bs[GE + k][v] += flip_sign(qi[v], mk[GE + k], r);
+                            for (int v = 0; v < V; ++v)
+                                bs[k][v] += flip_sign(qr[v], mk[k], r);
+#pragma unroll
+                        for (int k = 0; k < GO; ++k)
+#pragma unroll
+                            for (int v = 0; v < V; ++v)
+                                bs[GE + k][v] += flip_sign(qi[v], mk[GE + k], r);
+                    }
                 }
             }
 #pragma unroll

@@ -43,10 +43,18 @@ struct fpg_operator
     std::vector<fpg::Group> groups;
     std::vector<fpg::Chunk> chunks;
     std::vector<int> class_begin; // chunks of class c: [class_begin[c], class_begin[c+1])
+    // per-call decomposition: groups of >= kWhtMinStrings strings go to the
+    // transform kernel (wht), the rest to the direct classes (fast_chunks)
+    std::vector<fpg::Chunk> fast_chunks;
+    std::vector<int> fast_class_begin;
+    std::vector<fpg::WhtChunk> wht;
+    int wht_max_count = 0;
     fpg::StringRec *d_recs = nullptr;
     int32_t *d_orig = nullptr;
     fpg::Group *d_groups = nullptr;
     fpg::Chunk *d_chunks = nullptr;
+    fpg::Chunk *d_fast_chunks = nullptr;
+    fpg::WhtChunk *d_wht = nullptr;
 
     fpg::DevOp dev() const
     {

@@ -172,8 +172,12 @@ typedef struct fpg_batch fpg_batch;
 typedef struct fpg_batch_tuning
 {
     int32_t threads_per_cta; /* 128 or 256                                          */
-    int32_t ctas_per_sm;     /* CTAs per SM of each persistent grid, 1..8          */
-    int32_t rows_per_item;   /* rows of one work item, power of two >= 32          */
+    int32_t ctas_per_sm;     /* CTAs per SM of each persistent grid, 1..8; 0 = as
+                                many as the kernel's residency allows (default);
+                                -1 = item grid: one CTA per work item, drained by
+                                the hardware block scheduler                        */
+    int32_t rows_per_item;   /* row window of one work item when a problem's column
+                                tile exceeds tile_mb (power of two >= 32)          */
     int32_t tile_mb;         /* column-tile budget (MiB) for L2 residency, >= 1   */
 } fpg_batch_tuning;
 
@@ -181,7 +185,7 @@ int fpg_batch_create(int32_t dtype, fpg_batch **out);
 int fpg_batch_add(fpg_batch *batch, const fpg_operator *op, const void *coeffs, int64_t n_operators,
                   const void *states, void *out, int64_t n_states);
 /* Build the work queue and per-problem partial tables (allocates device memory).
- * tuning NULL: the batch's current tuning (defaults 256 / 4 / 4096). */
+ * tuning NULL: the batch's current tuning (defaults 256 / 0 / 32768 / 40). */
 int fpg_batch_plan(fpg_batch *batch, const fpg_batch_tuning *tuning);
 /* Enqueue one run on stream (plans first if needed). */
 int fpg_batch_run(fpg_batch *batch, void *stream);
