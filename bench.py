@@ -168,6 +168,7 @@ def run_ours(args, rank, world, dist):
 
     import fast_pauli as fp
     from fast_pauli import _abi
+    from fast_pauli import distributed as fdist
 
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
@@ -223,10 +224,7 @@ def run_ours(args, rank, world, dist):
         dist.barrier()
     launches = _abi.kernel_launches() - n0
     t_step = e0.elapsed_time(e1) / 1000.0 / args.steps
-    if dist:
-        tt = torch.tensor([t_step], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
+    t_step = fdist.max_over_ranks(t_step, dist)
     # dominant stage alone (per-string expectation kernels), same stream
     t_expect = time_device(expect_stage, args.steps, 2)
     clk = clocks.stop() if clocks else None

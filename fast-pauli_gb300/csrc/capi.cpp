@@ -194,6 +194,8 @@ void free_dev(fpg_operator *op)
     cudaFree(op->d_chunks);
     cudaFree(op->d_fast_chunks);
     cudaFree(op->d_wht);
+    cudaFree(op->d_pairs);
+    op->d_pairs = nullptr;
     op->d_recs = nullptr;
     op->d_orig = nullptr;
     op->d_groups = nullptr;
@@ -202,19 +204,35 @@ void free_dev(fpg_operator *op)
     op->d_wht = nullptr;
 }
 
-// Per-call decomposition: large x-groups -> transform-kernel chunks, the
-// rest -> direct-kernel chunks bucketed by class.
+// Per-call decomposition: large x-groups -> transform-kernel chunks; small
+// groups whose signs use one row bit at most -> pair-kernel chunks; the rest
+// -> direct-kernel chunks bucketed by class.
 void build_fast_decomposition(fpg_operator *op)
 {
     op->wht.clear();
     op->wht_max_count = 0;
+    op->pairs.clear();
     std::vector<std::vector<Chunk>> by_class(kNumChunkClasses);
-    std::vector<char> is_wht(op->groups.size(), 0);
+    std::vector<char> is_wht(op->groups.size(), 0); // 1: transform kernel, 2: pair kernel
     for (size_t gi = 0; gi < op->groups.size(); ++gi)
     {
         const Group &g = op->groups[gi];
         if (g.count < kWhtMinStrings)
+        {
+            // pair kernel when every sign, the pairing bit (top bit of x) dropped,
+            // uses <= 1 row bit
+            if (g.count > kPairMaxStrings)
+                continue;
+            const uint64_t pbit = g.x ? (1ull << (63 - __builtin_clzll(g.x))) : 0ull;
+            uint64_t bits = 0; // union of the strings' z'; one bit at most -> each z' in {0, e_a}
+            for (int32_t s = g.begin; s < g.begin + g.count; ++s)
+                bits |= op->recs[(size_t)s].z & ~pbit;
+            if (__builtin_popcountll(bits) > 1)
+                continue;
+            is_wht[gi] = 2;
+            op->pairs.push_back(PairChunk{g.x, g.begin, g.count, bits ? __builtin_ctzll(bits) : -1, 0});
             continue;
+        }
         is_wht[gi] = 1;
         int32_t n_even_total = 0;
         while (n_even_total < g.count && (op->recs[(size_t)(g.begin + n_even_total)].meta & 1u) == 0)
@@ -305,8 +323,8 @@ ExpectPlan plan_expect(const fpg_operator *op, int64_t S, bool fp32, const void 
     const int TR = 256 / p.TC;
     p.wht_TC = column_lanes_for_l2(pick_tc(S), op->n, fp32 ? 8 : 16, kColumnTileBytes);
     p.wht_ctiles = (int)((S + p.wht_TC - 1) / p.wht_TC);
-    const int64_t ctas =
-        (int64_t)op->fast_chunks.size() * p.n_ctiles + (int64_t)op->wht.size() * p.wht_ctiles;
+    const int64_t ctas = (int64_t)(op->fast_chunks.size() + op->pairs.size()) * p.n_ctiles +
+                         (int64_t)op->wht.size() * p.wht_ctiles;
     const int64_t NB = op->n >= 5 ? ((int64_t)1 << (op->n - 5)) : 1;
     const int64_t target = 152 * 8; // CTAs in flight: ~8 resident per SM
     int64_t splits = (target + ctas - 1) / std::max<int64_t>(ctas, 1);
@@ -336,6 +354,8 @@ int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int6
     if (!op->wht.empty())
         FPG_CUDA(launch_expect_wht(fp32, psi, S, op->n, dop, op->d_wht, (int)op->wht.size(), op->wht_max_count,
                                    plan.wht_TC, plan.wht_ctiles, plan.n_splits, dst, st));
+    if (!op->pairs.empty())
+        FPG_CUDA(launch_expect_pair(fp32, psi, S, op->n, dop, op->d_pairs, (int)op->pairs.size(), plan, dst, st));
     for (int c = 0; c < kNumChunkClasses; ++c)
     {
         const int b = op->fast_class_begin[(size_t)c], e = op->fast_class_begin[(size_t)c + 1];
@@ -480,6 +500,8 @@ extern "C"
             e = upload(&op->d_fast_chunks, op->fast_chunks);
         if (e == cudaSuccess)
             e = upload(&op->d_wht, op->wht);
+        if (e == cudaSuccess)
+            e = upload(&op->d_pairs, op->pairs);
         if (e != cudaSuccess)
         {
             free_dev(op);
@@ -539,8 +561,14 @@ extern "C"
             // 16-point transform: 4 adds per row per part; one add per string per 16 rows
             adds += rows * 4 * parts + (rows / 16) * w.count;
         }
+        for (const PairChunk &pc : op->pairs)
+        {
+            const bool paired = pc.x != 0; // rows paired across or inside 32-row blocks
+            const int64_t rows = paired ? D / 2 : D;
+            visits += rows; // four FMAs per row, the running sums included: no sign adds
+        }
         if (n_chunks)
-            *n_chunks = (int64_t)(op->fast_chunks.size() + op->wht.size());
+            *n_chunks = (int64_t)(op->fast_chunks.size() + op->wht.size() + op->pairs.size());
         if (row_visits)
             *row_visits = visits;
         if (sign_adds)

@@ -64,6 +64,19 @@ struct WhtChunk
 constexpr int kWhtMinStrings = 10;
 constexpr int kWhtMaxStrings = 128;
 
+// Work unit of the pair kernel (k_expect_pair.cu): a whole x-group of at most
+// kPairMaxStrings strings [begin, begin + count) whose signs, after dropping
+// the pairing bit (top bit of x), use at most row bit `abit` (-1: none).
+struct PairChunk
+{
+    uint64_t x;
+    int32_t begin;
+    int32_t count;
+    int32_t abit;
+    int32_t pad;
+};
+constexpr int kPairMaxStrings = 16;
+
 // Device-side view of an encoded operator.
 struct DevOp
 {
@@ -132,6 +145,11 @@ cudaError_t launch_expect_chunks(bool fp32, const void *psi, int64_t S, int n, c
                                  int n_chunks, int cls, const ExpectPlan &plan, double *ev_or_partial,
                                  cudaStream_t st);
 cudaError_t launch_reduce_splits(const double *partial, int n_splits, int64_t count, double *ev, cudaStream_t st);
+
+// Pair kernel over pair chunks; uses plan.TC / V / n_ctiles / n_splits like the
+// direct kernel and writes like it.
+cudaError_t launch_expect_pair(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const PairChunk *d_chunks,
+                               int n_chunks, const ExpectPlan &plan, double *out, cudaStream_t st);
 
 // Transform kernel over WHT chunks (128 threads = TC column lanes x 128/TC row
 // lanes, one complex element per lane); writes like launch_expect_chunks.

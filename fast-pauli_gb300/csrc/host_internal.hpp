@@ -49,6 +49,8 @@ struct fpg_operator
     std::vector<int> fast_class_begin;
     std::vector<fpg::WhtChunk> wht;
     int wht_max_count = 0;
+    std::vector<fpg::PairChunk> pairs; // groups served by the pair kernel
+    fpg::PairChunk *d_pairs = nullptr;
     fpg::StringRec *d_recs = nullptr;
     int32_t *d_orig = nullptr;
     fpg::Group *d_groups = nullptr;

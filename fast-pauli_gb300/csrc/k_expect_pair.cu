@@ -1,0 +1,241 @@
+// k_expect_pair.cu -- per-string expectation values for x-groups whose sign
+// patterns depend on at most one row bit.
+//
+// Same quantity as k_expect.cu (the per-string stage of
+// SummedPauliOp::expectation_value, fast_pauli/cpp/include/__summed_pauli_op.hpp:572-577).
+// For a group with x != 0 the rows i with the top bit p of x clear are
+// paired with i ^ x (each pair counts twice, Pauli strings being Hermitian);
+// a string's sign on those rows is (-1)^popc(i & z') with z' = z without
+// bit p.  When every string of the group has z' in {0, e_a}
+// for one bit a (e.g. the four strings XX, XY, YX, YY on two qubits), all of
+// them are combinations of four sums,
+//     U_c^re = sum_{i: bit a of i = c} Re q(i),  U_c^im likewise with Im q,
+// W(0) = U_0 + U_1 and W(e_a) = U_0 - U_1, and the sums are accumulated with
+// fused multiply-adds straight from the amplitudes:
+//     U^re += a_r b_r + a_i b_i,  U^im += a_r b_i - a_i b_r
+// -- four FMAs per row pair for the whole group, against q (4 operations)
+// plus one signed add per string (4 more) in the direct kernel.  The x = 0
+// group (diagonal strings) is summed over all rows.
+//
+// Layout as k_expect.cu: TC column lanes (V elements each) x (256 / TC) row
+// lanes, 32-row blocks, grid (chunks, row splits, column tiles).  For
+// x >= 32 whole blocks are paired (p >= 5); for 0 < x < 32 the pairs lie
+// inside a block and only its 16 rows with bit p clear are visited.  Rows
+// with bit a clear and set are visited side by side when a < 5; for a >= 5
+// bit a is constant over a block.  float32: block sums in float32,
+// Kahan-compensated across blocks, float64 across threads.
+#include "expect_body.cuh"
+
+namespace fpg
+{
+namespace
+{
+
+template <typename T, int V>
+__device__ __forceinline__ void fma_pair(const T (&ar)[V], const T (&ai)[V], const T (&br)[V], const T (&bi)[V],
+                                         T (&sre)[V], T (&sim)[V])
+{
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+    {
+        sre[v] = fma(ar[v], br[v], fma(ai[v], bi[v], sre[v]));
+        sim[v] = fma(ar[v], bi[v], fma(-ai[v], br[v], sim[v]));
+    }
+}
+
+template <typename T> __device__ __forceinline__ void kahan_add(T &acc, T &cmp, T x)
+{
+    if constexpr (sizeof(T) == 8)
+    {
+        acc += x;
+    }
+    else
+    {
+        const T y = x - cmp;
+        const T s = acc + y;
+        cmp = (s - acc) - y;
+        acc = s;
+    }
+}
+
+template <typename T, int V> constexpr int kPairMinBlocks = sizeof(T) == 4 ? 3 : 1;
+
+template <typename T, int V>
+__global__ void __launch_bounds__(256, kPairMinBlocks<T, V>)
+    k_expect_pair(const T *__restrict__ psi, int64_t S, int n, const StringRec *__restrict__ recs,
+                  const int32_t *__restrict__ orig, int64_t P, const PairChunk *__restrict__ chunks, int TC,
+                  int n_splits, double *__restrict__ out)
+{
+    extern __shared__ double red[]; // blockDim.x * V doubles
+    const PairChunk ch = chunks[blockIdx.x];
+    const int tid = threadIdx.x;
+    const int tc = tid & (TC - 1);
+    const int tr = tid / TC;
+    const int TR = blockDim.x / TC;
+    const int64_t t0 = ((int64_t)blockIdx.z * TC + tc) * V;
+    const bool col_ok = t0 < S;
+
+    const uint64_t D = 1ull << n;
+    const uint64_t xh = ch.x & ~31ull;
+    const uint32_t xl = (uint32_t)ch.x & 31u;
+    const bool paired = xh != 0;                                // blocks paired
+    const int pl = (!paired && xl != 0u) ? (31 - __clz((int)xl)) : -1; // rows paired inside a block
+    const int64_t NB = n >= 5 ? (int64_t)(D >> 5) : 1;
+    const int RB = n >= 5 ? 32 : (int)D;
+    const int64_t nblk = paired ? NB / 2 : NB;
+    const int hb = paired ? (63 - __clzll((long long)(xh >> 5))) : 0;
+    const int64_t per = (nblk + n_splits - 1) / n_splits;
+    const int64_t b0 = (int64_t)blockIdx.y * per;
+    const int64_t b1 = min(nblk, b0 + per);
+    const int abit = ch.abit; // -1: every string has z' = 0
+    const bool split_in_block = abit >= 0 && abit < 5;
+    // rows of a block visited: insert zero bits at pl and (a < 5) at a into
+    // m = 0 .. 2^free - 1, lower excluded bit first
+    const int e1 = split_in_block && pl >= 0 ? min(abit, pl) : (split_in_block ? abit : pl);
+    const int e2 = split_in_block && pl >= 0 ? max(abit, pl) : -1;
+    const int n_rows = 32 >> ((e1 >= 0) + (e2 >= 0));
+
+    // accumulators [c][v]: U_c^re, U_c^im with Kahan compensation (float32)
+    T ure[2][V], uim[2][V], cre[2][V], cim[2][V];
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+            ure[c][v] = uim[c][v] = cre[c][v] = cim[c][v] = T(0);
+
+    if (col_ok)
+    {
+        for (int64_t m = b0 + tr; m < b1; m += TR)
+        {
+            const uint64_t um = (uint64_t)m;
+            const uint64_t beta = paired ? (((um >> hb) << (hb + 1)) | (um & ((1ull << hb) - 1ull))) : um;
+            const uint64_t base = beta << 5;
+            const uint64_t baseB = base ^ xh;
+            T sre[2][V], sim[2][V];
+#pragma unroll
+            for (int c = 0; c < 2; ++c)
+#pragma unroll
+                for (int v = 0; v < V; ++v)
+                    sre[c][v] = sim[c][v] = T(0);
+#pragma unroll 4
+            for (int m2 = 0; m2 < n_rows; ++m2)
+            {
+                uint32_t r0 = (uint32_t)m2;
+                if (e1 >= 0)
+                    r0 = ((r0 >> e1) << (e1 + 1)) | (r0 & ((1u << e1) - 1u));
+                if (e2 >= 0)
+                    r0 = ((r0 >> e2) << (e2 + 1)) | (r0 & ((1u << e2) - 1u));
+                if ((int)r0 < RB)
+                {
+                    T ar[V], ai[V], br[V], bi[V];
+                    load_cvec<T, V>(psi + 2 * ((int64_t)(base + r0) * S + t0), ar, ai);
+                    load_cvec<T, V>(psi + 2 * ((int64_t)(baseB + (r0 ^ xl)) * S + t0), br, bi);
+                    if (split_in_block)
+                    {
+                        // r1 = r0 | 2^a < RB as a < n
+                        const uint32_t r1 = r0 | (1u << abit);
+                        T cr[V], ci[V], dr[V], di[V];
+                        load_cvec<T, V>(psi + 2 * ((int64_t)(base + r1) * S + t0), cr, ci);
+                        load_cvec<T, V>(psi + 2 * ((int64_t)(baseB + (r1 ^ xl)) * S + t0), dr, di);
+                        fma_pair<T, V>(cr, ci, dr, di, sre[1], sim[1]);
+                    }
+                    fma_pair<T, V>(ar, ai, br, bi, sre[0], sim[0]);
+                }
+            }
+            // block sums into the running sums: bit a of the block base picks
+            // the accumulator when a >= 5
+            const int c0 = (abit >= 5) ? (int)((base >> abit) & 1u) : 0;
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+            {
+                if (c0 == 0)
+                {
+                    kahan_add(ure[0][v], cre[0][v], sre[0][v]);
+                    kahan_add(uim[0][v], cim[0][v], sim[0][v]);
+                }
+                else
+                {
+                    kahan_add(ure[1][v], cre[1][v], sre[0][v]);
+                    kahan_add(uim[1][v], cim[1][v], sim[0][v]);
+                }
+                if (split_in_block)
+                {
+                    kahan_add(ure[1][v], cre[1][v], sre[1][v]);
+                    kahan_add(uim[1][v], cim[1][v], sim[1][v]);
+                }
+            }
+        }
+    }
+
+    // reduce the four sums over the row lanes (float64, fixed order), then
+    // thread row 0 writes every string of the chunk
+    const int W = TC * V;
+    double tot[4][V];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+    {
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+        {
+            const T a = q == 0 ? ure[0][v] : q == 1 ? ure[1][v] : q == 2 ? uim[0][v] : uim[1][v];
+            const T c = q == 0 ? cre[0][v] : q == 1 ? cre[1][v] : q == 2 ? cim[0][v] : cim[1][v];
+            red[tr * W + tc * V + v] = (double)a - (double)c;
+        }
+        __syncthreads();
+        for (int s = TR >> 1; s > 0; s >>= 1)
+        {
+            if (tr < s)
+#pragma unroll
+                for (int v = 0; v < V; ++v)
+                    red[tr * W + tc * V + v] += red[(tr + s) * W + tc * V + v];
+            __syncthreads();
+        }
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+            tot[q][v] = red[tc * V + v];
+        __syncthreads();
+    }
+    if (tr != 0 || !col_ok)
+        return;
+    const uint64_t pbit = paired ? (1ull << (hb + 5)) : (pl >= 0 ? (1ull << pl) : 0ull); // top bit of x
+    for (int k = 0; k < ch.count; ++k)
+    {
+        const int sidx = ch.begin + k;
+        const StringRec rec = recs[sidx];
+        const bool odd = (rec.meta & 1u) != 0;
+        const bool flip = ((rec.z & ~pbit) != 0); // z' = e_a
+        const int ny = (int)(rec.meta & 3u);
+        const double f = ((ny & 2) ? -1.0 : 1.0) * (pbit ? 2.0 : 1.0);
+        double *dst = out + ((int64_t)blockIdx.y * P + orig[sidx]) * S + t0;
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+        {
+            const double u0 = odd ? tot[2][v] : tot[0][v];
+            const double u1 = odd ? tot[3][v] : tot[1][v];
+            dst[v] = f * (flip ? u0 - u1 : u0 + u1);
+        }
+    }
+}
+
+} // namespace
+
+cudaError_t launch_expect_pair(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const PairChunk *d_chunks,
+                               int n_chunks, const ExpectPlan &plan, double *out, cudaStream_t st)
+{
+    if (n_chunks <= 0)
+        return cudaSuccess;
+    dim3 grid((unsigned)n_chunks, (unsigned)plan.n_splits, (unsigned)plan.n_ctiles);
+    const size_t smem = 256 * plan.V * sizeof(double);
+    if (!fp32)
+        k_expect_pair<double, 1><<<grid, 256, smem, st>>>((const double *)psi, S, n, op.recs, op.orig, op.P, d_chunks,
+                                                          plan.TC, plan.n_splits, out);
+    else if (plan.V == 2)
+        k_expect_pair<float, 2><<<grid, 256, smem, st>>>((const float *)psi, S, n, op.recs, op.orig, op.P, d_chunks,
+                                                         plan.TC, plan.n_splits, out);
+    else
+        k_expect_pair<float, 1><<<grid, 256, smem, st>>>((const float *)psi, S, n, op.recs, op.orig, op.P, d_chunks,
+                                                         plan.TC, plan.n_splits, out);
+    return launched();
+}
+
+} // namespace fpg

@@ -125,8 +125,10 @@ __global__ void __launch_bounds__(128)
                     {
                         const CT a = __ldg(ps + (int64_t)(base + r) * S + t0);
                         const CT b = __ldg(ps + (int64_t)(baseB + (uint64_t)(r ^ xl)) * S + t0);
-                        vre[r] = fma(a.x, b.x, a.y * b.y);
-                        vim[r] = fma(a.x, b.y, -(a.y * b.x));
+                        if (need_re)
+                            vre[r] = fma(a.x, b.x, a.y * b.y);
+                        if (need_im)
+                            vim[r] = fma(a.x, b.y, -(a.y * b.x));
                     }
             }
         }

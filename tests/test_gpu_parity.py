@@ -104,6 +104,61 @@ def test_weight2_strings_summed_expectation(n, S):
     assert normwise(got, oracle.summed_expectation(strings, h, psi)) < TOL_C128
 
 
+def _masks_to_string(n, x, z):
+    # row bit r <-> character n-1-r
+    ch = {(0, 0): "I", (1, 0): "X", (1, 1): "Y", (0, 1): "Z"}
+    return "".join(ch[((x >> (n - 1 - q)) & 1, (z >> (n - 1 - q)) & 1)] for q in range(n))
+
+
+def _pair_group_strings(rng, n, n_groups):
+    """x-groups whose signs, without the pairing bit (top bit of x), use one
+    row bit at most: the shape the pair kernel takes.  Sign bits below and
+    above the 32-row block, rows paired across blocks (x >= 32) and inside
+    them (x < 32), the diagonal group (x = 0) and groups without any sign
+    bit are all drawn."""
+    out = []
+    xs = {0}
+    while len(xs) < n_groups:
+        w = int(rng.integers(1, min(3, n) + 1))
+        xs.add(int(sum(1 << int(b) for b in rng.choice(n, size=w, replace=False))))
+    for x in sorted(xs):
+        pbit = (1 << (x.bit_length() - 1)) if x else 0
+        a = int(rng.integers(-1, n))
+        if a >= 0 and (1 << a) == pbit:
+            a = -1
+        zs = {0, pbit}
+        if a >= 0:
+            zs |= {1 << a, (1 << a) | pbit}
+        # every string of the group: x fixed, z' in {0, e_a}
+        cands = sorted(zs)
+        k = int(rng.integers(1, len(cands) + 1))
+        for z in rng.choice(cands, size=k, replace=False):
+            out.append(_masks_to_string(n, x, int(z)))
+    return out
+
+
+@pytest.mark.parametrize("n", [3, 4, 6, 9, 13])
+def test_pair_kernel_groups_per_string(n):
+    torch = pytest.importorskip("torch")
+    from fast_pauli import _abi
+
+    L = _abi.lib()
+    rng = np.random.default_rng(500 + n)
+    strings = _pair_group_strings(rng, n, min(12, (1 << n) - 1))
+    P, S = len(strings), 6
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    want = np.stack([oracle.string_expectation(s, psi).real for s in strings])
+    op = _abi.Operator(strings)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for dtype, tdt, tol in ((_abi.FPG_C128, torch.complex128, 1e-13), (_abi.FPG_C64, torch.complex64, 2e-6)):
+        dpsi = torch.from_numpy(psi).to(tdt).cuda()
+        ev = torch.empty((P, S), dtype=torch.float64, device="cuda")
+        _abi.check(L.fpg_expect_strings(op.handle, dpsi.data_ptr(), ev.data_ptr(), S, dtype, st))
+        torch.cuda.synchronize()
+        assert np.abs(ev.cpu().numpy() - want).max() < tol, dtype
+    op.close()
+
+
 def test_exhaustive_small_strings_vs_dense():
     rng = np.random.default_rng(3)
     for n in (1, 2, 3):
