@@ -196,6 +196,12 @@ void free_dev(fpg_operator *op)
     cudaFree(op->d_wht);
     cudaFree(op->d_pairs);
     op->d_pairs = nullptr;
+    cudaFree(op->d_margs);
+    op->d_margs = nullptr;
+    cudaFree(op->d_local);
+    op->d_local = nullptr;
+    cudaFree(op->d_glob);
+    op->d_glob = nullptr;
     op->d_recs = nullptr;
     op->d_orig = nullptr;
     op->d_groups = nullptr;
@@ -204,35 +210,54 @@ void free_dev(fpg_operator *op)
     op->d_wht = nullptr;
 }
 
-// Per-call decomposition: large x-groups -> transform-kernel chunks; small
-// groups whose signs use one row bit at most -> pair-kernel chunks; the rest
-// -> direct-kernel chunks bucketed by class.
+// Per-call decomposition of the x-groups, by the signs z' (z with the pairing
+// bit dropped) of their strings:
+//   all z' in {0, e_a}, <= kPairMaxStrings strings   -> pair kernel;
+//   every z' of <= 1 bit, >= kMargMinStrings strings -> marginal kernel;
+//   >= kWhtMinStrings strings                        -> transform kernel;
+//   the rest -> direct-kernel chunks bucketed by class.
 void build_fast_decomposition(fpg_operator *op)
 {
     op->wht.clear();
     op->wht_max_count = 0;
     op->pairs.clear();
+    op->margs.clear();
+    op->marg_max_high = 0;
     std::vector<std::vector<Chunk>> by_class(kNumChunkClasses);
-    std::vector<char> is_wht(op->groups.size(), 0); // 1: transform kernel, 2: pair kernel
+    std::vector<char> is_wht(op->groups.size(), 0); // 1: transform, 2: pair, 3: marginal kernel
     for (size_t gi = 0; gi < op->groups.size(); ++gi)
     {
         const Group &g = op->groups[gi];
-        if (g.count < kWhtMinStrings)
+        // signs with the pairing bit (top bit of x) dropped: z' of each string
+        const uint64_t pbit = g.x ? (1ull << (63 - __builtin_clzll(g.x))) : 0ull;
+        uint64_t bits = 0; // union of the z'
+        bool single = true; // every z' has at most one bit
+        int flags = 0;
+        for (int32_t s = g.begin; s < g.begin + g.count; ++s)
         {
-            // pair kernel when every sign, the pairing bit (top bit of x) dropped,
-            // uses <= 1 row bit
-            if (g.count > kPairMaxStrings)
-                continue;
-            const uint64_t pbit = g.x ? (1ull << (63 - __builtin_clzll(g.x))) : 0ull;
-            uint64_t bits = 0; // union of the strings' z'; one bit at most -> each z' in {0, e_a}
-            for (int32_t s = g.begin; s < g.begin + g.count; ++s)
-                bits |= op->recs[(size_t)s].z & ~pbit;
-            if (__builtin_popcountll(bits) > 1)
-                continue;
+            const StringRec &r = op->recs[(size_t)s];
+            bits |= r.z & ~pbit;
+            single = single && __builtin_popcountll(r.z & ~pbit) <= 1;
+            flags |= (r.meta & 1u) ? 2 : 1;
+        }
+        if (g.count <= kPairMaxStrings && __builtin_popcountll(bits) <= 1)
+        {
+            // pair kernel: every z' in {0, e_a}
             is_wht[gi] = 2;
             op->pairs.push_back(PairChunk{g.x, g.begin, g.count, bits ? __builtin_ctzll(bits) : -1, 0});
             continue;
         }
+        const int high = __builtin_popcountll(bits & ~31ull);
+        if (single && g.count >= kMargMinStrings && high <= kMargMaxHighBits)
+        {
+            // marginal kernel: every z' in {0} u {e_b}
+            is_wht[gi] = 3;
+            op->margs.push_back(MargChunk{g.x, bits, g.begin, g.count, flags, 0});
+            op->marg_max_high = std::max(op->marg_max_high, high);
+            continue;
+        }
+        if (g.count < kWhtMinStrings)
+            continue; // direct kernel
         is_wht[gi] = 1;
         int32_t n_even_total = 0;
         while (n_even_total < g.count && (op->recs[(size_t)(g.begin + n_even_total)].meta & 1u) == 0)
@@ -266,6 +291,28 @@ void build_fast_decomposition(fpg_operator *op)
         op->fast_chunks.insert(op->fast_chunks.end(), by_class[(size_t)c].begin(), by_class[(size_t)c].end());
     }
     op->fast_class_begin[kNumChunkClasses] = (int)op->fast_chunks.size();
+
+    // family-local string order (each family may write its own partial table)
+    static const int fam_of[4] = {kFamDirect, kFamWht, kFamPair, kFamMarg}; // by is_wht value
+    op->local.assign((size_t)op->P, 0);
+    op->glob.clear();
+    op->glob.reserve((size_t)op->P);
+    for (int f = 0; f < kNumFam; ++f)
+    {
+        op->fam_begin[f] = (int64_t)op->glob.size();
+        for (size_t gi = 0; gi < op->groups.size(); ++gi)
+        {
+            if (fam_of[(int)is_wht[gi]] != f)
+                continue;
+            const Group &g = op->groups[gi];
+            for (int32_t s = g.begin; s < g.begin + g.count; ++s)
+            {
+                op->local[(size_t)s] = (int32_t)((int64_t)op->glob.size() - op->fam_begin[f]);
+                op->glob.push_back(op->orig[(size_t)s]);
+            }
+        }
+    }
+    op->fam_begin[kNumFam] = (int64_t)op->glob.size();
 }
 
 int check_dtype(int32_t dtype)
@@ -320,22 +367,54 @@ ExpectPlan plan_expect(const fpg_operator *op, int64_t S, bool fp32, const void 
     const int64_t lanes = (S + p.V - 1) / p.V;
     p.TC = column_lanes_for_l2(pick_tc(lanes), op->n, p.V * (fp32 ? 8 : 16), kColumnTileBytes);
     p.n_ctiles = (int)((S + (int64_t)p.TC * p.V - 1) / ((int64_t)p.TC * p.V));
-    const int TR = 256 / p.TC;
     p.wht_TC = column_lanes_for_l2(pick_tc(S), op->n, fp32 ? 8 : 16, kColumnTileBytes);
     p.wht_ctiles = (int)((S + p.wht_TC - 1) / p.wht_TC);
-    const int64_t ctas = (int64_t)(op->fast_chunks.size() + op->pairs.size()) * p.n_ctiles +
-                         (int64_t)op->wht.size() * p.wht_ctiles;
-    const int64_t NB = op->n >= 5 ? ((int64_t)1 << (op->n - 5)) : 1;
-    const int64_t target = 152 * 8; // CTAs in flight: ~8 resident per SM
-    int64_t splits = (target + ctas - 1) / std::max<int64_t>(ctas, 1);
-    const int bpl = p.V * (fp32 ? 8 : 16);
-    if (column_tile_footprint(p.TC, op->n, bpl) > kColumnTileBytes)
-        splits = std::max<int64_t>(splits, (NB / 2 + kWindowBlocks - 1) / kWindowBlocks); // L2 row window
-    const int64_t max_splits = std::max<int64_t>(1, NB / (2 * (int64_t)TR * 4)); // >= 4 blocks per row lane
-    splits = std::max<int64_t>(1, std::min(splits, max_splits));
-    splits = std::min<int64_t>(splits, 65535);
-    p.n_splits = (int)splits;
+    const int64_t NB = op->n >= 5 ? ((int64_t)1 << (op->n - 5)) : 1;    // 32-row blocks
+    const int64_t NB16 = op->n >= 4 ? ((int64_t)1 << (op->n - 4)) : 1;  // 16-row blocks (transform kernel)
+    const bool over = column_tile_footprint(p.TC, op->n, p.V * (fp32 ? 8 : 16)) > kColumnTileBytes;
+    const bool over1 = column_tile_footprint(p.wht_TC, op->n, fp32 ? 8 : 16) > kColumnTileBytes;
+    // row splits of one launch: enough CTAs for ~8 resident per SM, an L2 row
+    // window when even a one-line column tile does not fit, >= 4 blocks per
+    // row lane
+    auto pick = [](int64_t ctas_per_split, int64_t blocks, int row_lanes, bool windowed, int64_t window) {
+        if (ctas_per_split <= 0)
+            return 1;
+        const int64_t target = 152 * 8;
+        int64_t s = (target + ctas_per_split - 1) / ctas_per_split;
+        if (windowed)
+            s = std::max<int64_t>(s, (blocks + window - 1) / window);
+        const int64_t mx = std::max<int64_t>(1, blocks / ((int64_t)row_lanes * 4));
+        return (int)std::max<int64_t>(1, std::min<int64_t>(std::min(s, mx), 65535));
+    };
+    p.fam_splits[kFamDirect] =
+        pick((int64_t)op->fast_chunks.size() * p.n_ctiles, NB / 2, 256 / p.TC, over, kWindowBlocks);
+    p.fam_splits[kFamPair] = pick((int64_t)op->pairs.size() * p.n_ctiles, NB / 2, 256 / p.TC, over, kWindowBlocks);
+    p.fam_splits[kFamMarg] =
+        pick((int64_t)op->margs.size() * p.wht_ctiles, NB / 2, 256 / p.wht_TC, over1, kWindowBlocks);
+    p.fam_splits[kFamWht] =
+        pick((int64_t)op->wht.size() * p.wht_ctiles, NB16 / 2, 128 / p.wht_TC, over1, 2 * kWindowBlocks);
+    p.n_splits = 1;
+    for (int f = 0; f < kNumFam; ++f)
+        p.n_splits = std::max(p.n_splits, p.fam_splits[f]);
     return p;
+}
+
+// Scratch (doubles) of the families' partial tables; off[f] = offset of
+// family f's table, or -1 when it writes the caller-ordered table directly.
+int64_t family_partials(const fpg_operator *op, const ExpectPlan &plan, int64_t S, int64_t (&off)[kNumFam])
+{
+    int64_t total = 0;
+    for (int f = 0; f < kNumFam; ++f)
+    {
+        const int64_t Pf = op->fam_begin[f + 1] - op->fam_begin[f];
+        off[f] = -1;
+        if (plan.fam_splits[f] > 1 && Pf > 0)
+        {
+            off[f] = total;
+            total += (int64_t)plan.fam_splits[f] * Pf * S;
+        }
+    }
+    return total;
 }
 
 int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int64_t S, bool fp32, cudaStream_t st)
@@ -343,28 +422,56 @@ int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int6
     if (S <= 0 || op->P <= 0)
         return FPG_OK;
     const ExpectPlan plan = plan_expect(op, S, fp32, psi);
-    const DevOp dop = op->dev();
+    int64_t off[kNumFam];
+    const int64_t scratch = family_partials(op, plan, S, off);
     Scratch partial(st);
-    double *dst = ev;
-    if (plan.n_splits > 1)
-    {
-        FPG_CUDA(partial.alloc((size_t)plan.n_splits * (size_t)op->P * (size_t)S * sizeof(double)));
-        dst = (double *)partial.p;
-    }
+    if (scratch > 0)
+        FPG_CUDA(partial.alloc((size_t)scratch * sizeof(double)));
+    // family f writes ev directly (caller order) or its own partial table
+    // (family-local order, reduced below)
+    auto target = [&](int f, DevOp &d, ExpectPlan &pl) -> double * {
+        d = op->dev();
+        pl = plan;
+        pl.n_splits = plan.fam_splits[f];
+        if (off[f] < 0)
+            return ev;
+        d.orig = op->d_local;
+        d.P = op->fam_begin[f + 1] - op->fam_begin[f];
+        return (double *)partial.p + off[f];
+    };
+    DevOp d;
+    ExpectPlan pl;
     if (!op->wht.empty())
-        FPG_CUDA(launch_expect_wht(fp32, psi, S, op->n, dop, op->d_wht, (int)op->wht.size(), op->wht_max_count,
-                                   plan.wht_TC, plan.wht_ctiles, plan.n_splits, dst, st));
-    if (!op->pairs.empty())
-        FPG_CUDA(launch_expect_pair(fp32, psi, S, op->n, dop, op->d_pairs, (int)op->pairs.size(), plan, dst, st));
-    for (int c = 0; c < kNumChunkClasses; ++c)
     {
-        const int b = op->fast_class_begin[(size_t)c], e = op->fast_class_begin[(size_t)c + 1];
-        if (e > b)
-            FPG_CUDA(
-                launch_expect_chunks(fp32, psi, S, op->n, dop, op->d_fast_chunks + b, e - b, c, plan, dst, st));
+        double *dst = target(kFamWht, d, pl);
+        FPG_CUDA(launch_expect_wht(fp32, psi, S, op->n, d, op->d_wht, (int)op->wht.size(), op->wht_max_count,
+                                   pl.wht_TC, pl.wht_ctiles, pl.n_splits, dst, st));
     }
-    if (plan.n_splits > 1)
-        FPG_CUDA(launch_reduce_splits(dst, plan.n_splits, op->P * S, ev, st));
+    if (!op->margs.empty())
+    {
+        double *dst = target(kFamMarg, d, pl);
+        FPG_CUDA(launch_expect_marg(fp32, psi, S, op->n, d, op->d_margs, (int)op->margs.size(), op->marg_max_high,
+                                    pl.wht_TC, pl.wht_ctiles, pl.n_splits, dst, st));
+    }
+    if (!op->pairs.empty())
+    {
+        double *dst = target(kFamPair, d, pl);
+        FPG_CUDA(launch_expect_pair(fp32, psi, S, op->n, d, op->d_pairs, (int)op->pairs.size(), pl, dst, st));
+    }
+    {
+        double *dst = target(kFamDirect, d, pl);
+        for (int c = 0; c < kNumChunkClasses; ++c)
+        {
+            const int b = op->fast_class_begin[(size_t)c], e = op->fast_class_begin[(size_t)c + 1];
+            if (e > b)
+                FPG_CUDA(launch_expect_chunks(fp32, psi, S, op->n, d, op->d_fast_chunks + b, e - b, c, pl, dst, st));
+        }
+    }
+    for (int f = 0; f < kNumFam; ++f)
+        if (off[f] >= 0)
+            FPG_CUDA(launch_reduce_family((const double *)partial.p + off[f], plan.fam_splits[f],
+                                          op->fam_begin[f + 1] - op->fam_begin[f], S, op->d_glob + op->fam_begin[f],
+                                          ev, st));
     return FPG_OK;
 }
 
@@ -386,9 +493,8 @@ size_t request_scratch_bytes(const fpg_operator *op, int64_t K, int64_t S, bool 
         return b + 4096;
     }
     const ExpectPlan plan = plan_expect(op, S, fp32, nullptr);
-    size_t b = P * (size_t)S * sizeof(double);
-    if (plan.n_splits > 1)
-        b += (size_t)plan.n_splits * P * (size_t)S * sizeof(double);
+    int64_t off[kNumFam];
+    size_t b = P * (size_t)S * sizeof(double) + (size_t)family_partials(op, plan, S, off) * sizeof(double);
     if (fp32)
         b += tc_workspace_bytes(2 * K, S, op->P);
     return b + 4096;
@@ -502,6 +608,12 @@ extern "C"
             e = upload(&op->d_wht, op->wht);
         if (e == cudaSuccess)
             e = upload(&op->d_pairs, op->pairs);
+        if (e == cudaSuccess)
+            e = upload(&op->d_margs, op->margs);
+        if (e == cudaSuccess)
+            e = upload(&op->d_local, op->local);
+        if (e == cudaSuccess)
+            e = upload(&op->d_glob, op->glob);
         if (e != cudaSuccess)
         {
             free_dev(op);
@@ -567,8 +679,15 @@ extern "C"
             const int64_t rows = paired ? D / 2 : D;
             visits += rows; // four FMAs per row, the running sums included: no sign adds
         }
+        for (const MargChunk &mc : op->margs)
+        {
+            const int64_t rows = mc.x != 0 ? D / 2 : D;
+            const int parts = ((mc.flags & 1) ? 1 : 0) + ((mc.flags & 2) ? 1 : 0);
+            visits += rows;
+            adds += rows * parts * 17 / 8; // marginal tree: 68 adds per 32 rows and part
+        }
         if (n_chunks)
-            *n_chunks = (int64_t)(op->fast_chunks.size() + op->wht.size() + op->pairs.size());
+            *n_chunks = (int64_t)(op->fast_chunks.size() + op->wht.size() + op->pairs.size() + op->margs.size());
         if (row_visits)
             *row_visits = visits;
         if (sign_adds)

@@ -77,6 +77,23 @@ struct PairChunk
 };
 constexpr int kPairMaxStrings = 16;
 
+// Work unit of the marginal kernel (k_expect_marg.cu): a whole x-group
+// [begin, begin + count) whose strings each have z' (z without the pairing
+// bit) of at most one bit; zmask = the union of the z', of which at most
+// kMargMaxHighBits bits lie at row bit 5 or above.  flags: bit 0 = the
+// group has strings with even #Y (needs Re q), bit 1 = odd #Y (Im q).
+struct MargChunk
+{
+    uint64_t x;
+    uint64_t zmask;
+    int32_t begin;
+    int32_t count;
+    int32_t flags;
+    int32_t pad;
+};
+constexpr int kMargMaxHighBits = 18;
+constexpr int kMargMinStrings = 4;
+
 // Device-side view of an encoded operator.
 struct DevOp
 {
@@ -130,26 +147,50 @@ inline int64_t column_tile_footprint(int tc, int n, int bytes_per_lane)
 // a window of at most this many 32-row blocks, which L2 can hold.
 constexpr int64_t kWindowBlocks = 1024;
 
+// Kernel families of the per-call decomposition; each picks its own row
+// splits so that every launch fills the GPU.
+enum
+{
+    kFamDirect = 0,
+    kFamPair = 1,
+    kFamMarg = 2,
+    kFamWht = 3,
+    kNumFam = 4
+};
+
 struct ExpectPlan
 {
     int TC;           // column lanes per CTA (power of two <= 32)
     int V;            // complex elements per lane (1 or 2)
     int n_ctiles;     // column tiles
-    int n_splits;     // row splits (>1 -> partial buffer + reduction)
-    int wht_TC;       // column lanes of the transform kernel (V = 1)
-    int wht_ctiles;   // its column tiles
+    int n_splits;     // row splits of a launch (>1 -> partial buffer + reduction)
+    int wht_TC;       // column lanes of the V = 1 kernels (transform, marginal)
+    int wht_ctiles;   // their column tiles
+    int fam_splits[kNumFam]; // per-call path: row splits of each family
 };
 
-// ev_or_partial: [n_splits][P][S] float64 (row-major).  One launch per class.
+// ev_or_partial: [n_splits][P][S] float64 (row-major), string index orig[s].
+// One launch per class.
 cudaError_t launch_expect_chunks(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const Chunk *d_chunks,
                                  int n_chunks, int cls, const ExpectPlan &plan, double *ev_or_partial,
                                  cudaStream_t st);
-cudaError_t launch_reduce_splits(const double *partial, int n_splits, int64_t count, double *ev, cudaStream_t st);
+// ev[glob[l] * S + t] = sum_p partial[(p * Pf + l) * S + t]: the partial table
+// of one kernel family (Pf strings in family-local order) into the caller-
+// ordered table.
+cudaError_t launch_reduce_family(const double *partial, int n_splits, int64_t Pf, int64_t S, const int32_t *glob,
+                                 double *ev, cudaStream_t st);
 
 // Pair kernel over pair chunks; uses plan.TC / V / n_ctiles / n_splits like the
 // direct kernel and writes like it.
 cudaError_t launch_expect_pair(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const PairChunk *d_chunks,
                                int n_chunks, const ExpectPlan &plan, double *out, cudaStream_t st);
+
+// Marginal kernel over marginal chunks: one complex element per lane, TC
+// column lanes (the V = 1 tiling, plan.wht_TC / wht_ctiles), 256 threads;
+// max_high_bits = the largest number of zmask bits >= 5 over the chunks.
+cudaError_t launch_expect_marg(bool fp32, const void *psi, int64_t S, int n, const DevOp &op,
+                               const MargChunk *d_chunks, int n_chunks, int max_high_bits, int TC, int n_ctiles,
+                               int n_splits, double *out, cudaStream_t st);
 
 // Transform kernel over WHT chunks (128 threads = TC column lanes x 128/TC row
 // lanes, one complex element per lane); writes like launch_expect_chunks.

@@ -51,6 +51,16 @@ struct fpg_operator
     int wht_max_count = 0;
     std::vector<fpg::PairChunk> pairs; // groups served by the pair kernel
     fpg::PairChunk *d_pairs = nullptr;
+    std::vector<fpg::MargChunk> margs; // groups served by the marginal kernel
+    int marg_max_high = 0;
+    fpg::MargChunk *d_margs = nullptr;
+    // strings by kernel family: local[s] = index of sorted string s within its
+    // family; glob[fam_begin[f] + l] = caller index of family f's string l
+    std::vector<int32_t> local;
+    std::vector<int32_t> glob;
+    int64_t fam_begin[fpg::kNumFam + 1] = {};
+    int32_t *d_local = nullptr;
+    int32_t *d_glob = nullptr;
     fpg::StringRec *d_recs = nullptr;
     int32_t *d_orig = nullptr;
     fpg::Group *d_groups = nullptr;

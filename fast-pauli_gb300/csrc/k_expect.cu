@@ -102,19 +102,34 @@ cudaError_t launch_v(const T *psi, int64_t S, int n, const DevOp &op, const Chun
     return launched();
 }
 
-__global__ void k_reduce_splits(const double *__restrict__ partial, int n_splits, int64_t count,
-                                double *__restrict__ ev)
+__global__ void k_reduce_family(const double *__restrict__ partial, int n_splits, int64_t Pf, int64_t S,
+                                const int32_t *__restrict__ glob, double *__restrict__ ev)
 {
+    const int64_t count = Pf * S;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x)
     {
         double s = 0.0;
         for (int p = 0; p < n_splits; ++p)
             s += partial[(int64_t)p * count + e];
-        ev[e] = s;
+        const int64_t l = e / S;
+        ev[(int64_t)glob[l] * S + (e - l * S)] = s;
     }
 }
 
 } // namespace
+
+cudaError_t launch_reduce_family(const double *partial, int n_splits, int64_t Pf, int64_t S, const int32_t *glob,
+                                 double *ev, cudaStream_t st)
+{
+    const int64_t count = Pf * S;
+    if (count <= 0)
+        return cudaSuccess;
+    int64_t blocks = (count + 255) / 256;
+    if (blocks > 152 * 16)
+        blocks = 152 * 16;
+    k_reduce_family<<<(unsigned)blocks, 256, 0, st>>>(partial, n_splits, Pf, S, glob, ev);
+    return launched();
+}
 
 cudaError_t launch_expect_chunks(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const Chunk *d_chunks,
                                  int n_chunks, int cls, const ExpectPlan &plan, double *out, cudaStream_t st)
@@ -126,17 +141,6 @@ cudaError_t launch_expect_chunks(bool fp32, const void *psi, int64_t S, int n, c
     if (plan.V == 2)
         return launch_v<float, 2>((const float *)psi, S, n, op, d_chunks, n_chunks, cls, plan, out, st);
     return launch_v<float, 1>((const float *)psi, S, n, op, d_chunks, n_chunks, cls, plan, out, st);
-}
-
-cudaError_t launch_reduce_splits(const double *partial, int n_splits, int64_t count, double *ev, cudaStream_t st)
-{
-    if (count <= 0)
-        return cudaSuccess;
-    int64_t blocks = (count + 255) / 256;
-    if (blocks > 152 * 16)
-        blocks = 152 * 16;
-    k_reduce_splits<<<(unsigned)blocks, 256, 0, st>>>(partial, n_splits, count, ev);
-    return launched();
 }
 
 } // namespace fpg

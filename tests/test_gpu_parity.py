@@ -159,6 +159,47 @@ def test_pair_kernel_groups_per_string(n):
     op.close()
 
 
+def _marginal_group_strings(rng, n, n_groups):
+    """x-groups of >= 4 strings whose z' (pairing bit dropped) each have at
+    most one bit, over several bits: the shape the marginal kernel takes
+    (e.g. X_a, Y_a, X_a Z_b, Y_a Z_b)."""
+    out = []
+    xs = {0}
+    while len(xs) < n_groups:
+        w = int(rng.integers(1, min(2, n) + 1))
+        xs.add(int(sum(1 << int(b) for b in rng.choice(n, size=w, replace=False))))
+    for x in sorted(xs):
+        pbit = (1 << (x.bit_length() - 1)) if x else 0
+        cands = [0] + [1 << b for b in range(n) if (1 << b) != pbit]
+        cands = cands + [c | pbit for c in cands] if pbit else cands
+        k = int(rng.integers(4, min(len(cands), 24) + 1))
+        for z in rng.choice(cands, size=k, replace=False):
+            out.append(_masks_to_string(n, x, int(z)))
+    return out
+
+
+@pytest.mark.parametrize("n,S", [(3, 5), (4, 2), (6, 7), (9, 33), (14, 3), (20, 2)])
+def test_marginal_kernel_groups_per_string(n, S):
+    torch = pytest.importorskip("torch")
+    from fast_pauli import _abi
+
+    L = _abi.lib()
+    rng = np.random.default_rng(700 + n)
+    strings = _marginal_group_strings(rng, n, min(6, (1 << n) - 1))
+    P = len(strings)
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    want = np.stack([oracle.string_expectation(s, psi).real for s in strings])
+    op = _abi.Operator(strings)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for dtype, tdt, tol in ((_abi.FPG_C128, torch.complex128, 1e-13), (_abi.FPG_C64, torch.complex64, 2e-6)):
+        dpsi = torch.from_numpy(psi).to(tdt).cuda()
+        ev = torch.empty((P, S), dtype=torch.float64, device="cuda")
+        _abi.check(L.fpg_expect_strings(op.handle, dpsi.data_ptr(), ev.data_ptr(), S, dtype, st))
+        torch.cuda.synchronize()
+        assert np.abs(ev.cpu().numpy() - want).max() < tol, dtype
+    op.close()
+
+
 def test_exhaustive_small_strings_vs_dense():
     rng = np.random.default_rng(3)
     for n in (1, 2, 3):
