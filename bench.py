@@ -245,8 +245,8 @@ def run_ours(args, rank, world, dist):
         "unit": "GB/s",
         "frac": alg_bytes_expect / t_expect / 1e9 / hbm,
         "peak_kind": peak_kind,
-        "traffic": _ncu_traffic("k_expect_chunks_config2_fp64.md"),
-        "kernel": "k_expect_chunks (fpg_expect_strings stage)",
+        "traffic": _ncu_traffic("expect_stage_config2_fp64.md"),
+        "kernel": "expectation stage (fpg_expect_strings: k_expect_pair + k_expect_marg + k_expect_wht)",
         "kernel_ms": t_expect * 1e3,
         "algorithmic_bytes_per_launch": alg_bytes_expect,
         "pipe": {"kind": "fp64", "ops_per_launch": fp64_ops, "achieved_tflops": 2 * fp64_ops / t_expect / 1e12,
@@ -471,6 +471,76 @@ def _cfg4_problems(seed=1004, count=256):
     return probs
 
 
+def run_square(args):
+    """SummedPauliOp.square of the configuration-2 operator set (n=14, 861
+    weight<=2 strings, K=1000) onto the 91771 strings of weight <= 4.
+    Metric: pair-terms/s = P^2 * K per call / time (the reference forms every
+    (i, j, k) term)."""
+    import numpy as np
+    import torch
+
+    import fast_pauli as fp
+    import oracle
+    from fast_pauli import _abi
+
+    torch.cuda.set_device(0)
+    n, K = 14, 1000
+    strings, h, _ = config2(n=n, K=K, S=1, seed=1002)
+    sq_strings = [str(s) for s in fp.helpers.calculate_pauli_strings_max_weight(n, 4)]
+    P, A = len(strings), len(sq_strings)
+    L = _abi.lib()
+    op, q = _abi.Operator(strings), _abi.Operator(sq_strings)
+    stream = _stream_handle()
+    dh = torch.from_numpy(h).cuda()
+    out = torch.empty((A, K), dtype=torch.complex128, device="cuda")
+
+    def step():
+        _abi.check(L.fpg_summed_square(op.handle, dh.data_ptr(), K, q.handle, out.data_ptr(), _abi.FPG_C128, stream))
+
+    n0 = _abi.kernel_launches()
+    t = time_device(step, args.steps, args.warmup)
+    launches = (_abi.kernel_launches() - n0) / (args.steps + args.warmup)
+    pair_terms = P * P * K
+    # end to end: the public API (host coefficients in, host SummedPauliOp out)
+    sop = fp.SummedPauliOp(strings, h)
+    sop.square()
+    t0 = time.perf_counter()
+    res = sop.square()
+    t_e2e = time.perf_counter() - t0
+    e2e_err = float(np.abs(res.coeffs.T - out.cpu().numpy()).max() / np.abs(out.cpu().numpy()).max())
+    # CPU baseline: the oracle port of the reference's square on K_s operators
+    Ks = 24
+    tc = time.perf_counter()
+    oracle.summed_square(strings, h[:, :Ks], sq_strings)
+    tc = time.perf_counter() - tc
+    ref_err = float(np.abs(oracle.summed_square(strings[:200], h[:200, :4], sq_strings)
+                           - _square_dev(L, _abi, strings[:200], h[:200, :4], sq_strings, stream)).max())
+    return {"metric": "square pair-terms/s", "value": pair_terms / t, "unit": "pair-terms/s",
+            "workload": f"SummedPauliOp.square float64: n={n}, {P} weight<=2 strings, K={K} -> {A} strings "
+                        "of weight <= 4", "ms_per_step": t * 1e3, "steps": args.steps, "warmup": args.warmup,
+            "launches_per_step": launches,
+            "e2e": {"value": pair_terms / t_e2e, "unit": "pair-terms/s", "ms": t_e2e * 1e3,
+                    "h2d_bytes": P * K * 16, "d2h_bytes": A * K * 16,
+                    "api": "fast_pauli.SummedPauliOp.square()", "max_rel_diff_vs_device_call": e2e_err},
+            "max_abs_err_vs_oracle_200_strings": ref_err,
+            "cpu_baseline": {"value": P * P * Ks / tc, "unit": "pair-terms/s", "cores": oracle.max_threads(),
+                             "kind": "port", "sample": f"all {P}^2 pairs, {Ks} of {K} operators ({tc:.2f} s)"}}
+
+
+def _square_dev(L, _abi, strings, h, sq_strings, stream):
+    import torch
+
+    op, q = _abi.Operator(strings), _abi.Operator(sq_strings)
+    dh = torch.from_numpy(h).cuda()
+    out = torch.empty((len(sq_strings), h.shape[1]), dtype=torch.complex128, device="cuda")
+    _abi.check(L.fpg_summed_square(op.handle, dh.data_ptr(), h.shape[1], q.handle, out.data_ptr(), _abi.FPG_C128,
+                                   stream))
+    res = out.cpu().numpy()
+    op.close()
+    q.close()
+    return res
+
+
 def run_batch(args):
     """Configuration 4: 256 uneven PauliOp.expectation_value problems in one
     persistent, graph-captured launch (tuning from the autotuner, tuned on the
@@ -648,8 +718,9 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-mixed", action="store_true")
-    ap.add_argument("--workload", default="summed", choices=["summed", "batch", "serve"],
-                    help="summed: configuration 2 (default line); batch: configuration 4; serve: configuration 5")
+    ap.add_argument("--workload", default="summed", choices=["summed", "batch", "serve", "square"],
+                    help="summed: configuration 2 (default line); batch: configuration 4; serve: configuration 5; "
+                         "square: SummedPauliOp.square of the configuration-2 operators")
     ap.add_argument("--requests", type=int, default=200, help="serve: number of requests")
     ap.add_argument("--rate", type=float, default=50.0, help="serve: Poisson arrival rate (requests/s)")
     ap.add_argument("--max-n", type=int, default=24, help="serve: largest qubit count")
@@ -665,7 +736,7 @@ def main():
         return
     if args.workload != "summed" and args.impl == "ours":
         if rank == 0:
-            line = run_batch(args) if args.workload == "batch" else run_serve(args)
+            line = {"batch": run_batch, "serve": run_serve, "square": run_square}[args.workload](args)
             print(json.dumps(line), flush=True)
         return
     if args.impl == "reference":

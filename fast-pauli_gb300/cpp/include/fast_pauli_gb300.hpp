@@ -1082,28 +1082,34 @@ template <std::floating_point T> struct SummedPauliOp
         return ops;
     }
 
-    // Square of each operator A_k -> A_k^2 (reference :197-268), host side.
+    // Square of each operator A_k -> A_k^2 (reference :197-268): the squared
+    // string set as the reference (all strings of weight <= min(n, 2 w)),
+    // coefficients from the GPU (fpg_summed_square).
     SummedPauliOp square() const
     {
         size_t weight = 0;
         for (auto const &p : pauli_strings)
             weight = std::max<size_t>(weight, p.weight);
         auto sq = calculate_pauli_strings_max_weight(n_qubits(), std::min(n_qubits(), 2 * weight));
-        std::unordered_map<PauliString, size_t> idx;
-        for (size_t a = 0; a < sq.size(); ++a)
-            idx[sq[a]] = a;
-        const size_t K = n_operators(), P = n_pauli_strings();
-        std::vector<std::complex<T>> out(sq.size() * K);
-        for (size_t i = 0; i < P; ++i)
-            for (size_t j = 0; j < P; ++j)
-            {
-                auto [ph, prod] = pauli_strings[i] * pauli_strings[j];
-                const size_t a = idx.at(prod);
-                const std::complex<T> phase(ph);
-                for (size_t k = 0; k < K; ++k)
-                    out[a * K + k] += phase * coeffs(i, k) * coeffs(j, k);
-            }
-        return SummedPauliOp(sq, Tensor<2>(out.data(), sq.size(), K));
+        using C = std::complex<T>;
+        const size_t K = n_operators(), A = sq.size();
+        std::vector<C> out(A * K);
+        if (!pauli_strings.empty() && K > 0 && A > 0)
+        {
+            fpg_operator *op = cache_.get(pauli_strings);
+            const std::string joined = detail::join_strings(sq);
+            fpg_operator *q = nullptr;
+            detail::check(fpg_operator_create(joined.data(), (int64_t)A, (int32_t)n_qubits(), &q));
+            detail::OpHandle qh(q);
+            cudaStream_t st = detail::stream();
+            detail::DevBuf dh = upload_coeffs<C>(st);
+            detail::DevBuf dout(A * K * sizeof(C), st);
+            detail::check(fpg_summed_square(op, dh.p, (int64_t)K, q, dout.p, detail::dtype_of<C>(), st));
+            detail::cuda_check(cudaMemcpyAsync(out.data(), dout.p, dout.bytes, cudaMemcpyDeviceToHost, st),
+                               "cudaMemcpyAsync");
+            detail::sync(st);
+        }
+        return SummedPauliOp(sq, Tensor<2>(out.data(), A, K));
     }
 
     template <typename View> void to_tensor(View A_k_out) const

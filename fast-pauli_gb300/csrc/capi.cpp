@@ -871,4 +871,47 @@ extern "C"
         return FPG_OK;
     }
 
+    int fpg_summed_square(const fpg_operator *op, const void *coeffs, int64_t n_operators, const fpg_operator *sq,
+                          void *out, int32_t dtype, void *stream)
+    {
+        if (!op || !sq)
+            return set_error(FPG_ERR_INVALID, "op and sq must not be null");
+        if (int rc = check_dtype(dtype))
+            return rc;
+        if (n_operators < 0)
+            return set_error(FPG_ERR_INVALID, "n_operators must be >= 0");
+        const int64_t P = op->P, A = sq->P, K = n_operators;
+        if (P > 0 && A > 0 && op->n != sq->n)
+            return set_error(FPG_ERR_INVALID, "op and sq must act on the same number of qubits");
+        if (A == 0 || K == 0)
+            return FPG_OK;
+        if (!out || (P > 0 && !coeffs))
+            return set_error(FPG_ERR_INVALID, "null array");
+        if (int rc = check_aligned(dtype, {coeffs, out}))
+            return rc;
+        if (square_max_terms(P) > ((int64_t)1 << 31))
+            return set_error(FPG_ERR_UNSUPPORTED, "too many strings to square");
+        DeviceGuard g(op->device);
+        if (!g.ok)
+            return set_error(FPG_ERR_CUDA, "cannot select the operator's device");
+        cudaStream_t st = (cudaStream_t)stream;
+        const bool fp32 = dtype == FPG_C64;
+        if (P == 0)
+        {
+            FPG_CUDA(cudaMemsetAsync(out, 0, (size_t)A * (size_t)K * (fp32 ? 8 : 16), st));
+            FPG_CUDA(cudaStreamSynchronize(st));
+            return FPG_OK;
+        }
+        Scratch ws(st);
+        FPG_CUDA(ws.alloc(square_workspace_bytes(P, A)));
+        unsigned long long *d_found = nullptr;
+        FPG_CUDA(launch_square(fp32, op->dev(), sq->dev(), coeffs, K, out, ws.p, &d_found, st));
+        unsigned long long found = 0;
+        FPG_CUDA(cudaMemcpyAsync(&found, d_found, sizeof(found), cudaMemcpyDeviceToHost, st));
+        FPG_CUDA(cudaStreamSynchronize(st));
+        if (found != (unsigned long long)P * (unsigned long long)P)
+            return set_error(FPG_ERR_INVALID, "a product of two strings is not among the squared strings");
+        return FPG_OK;
+    }
+
 } // extern "C"

@@ -234,6 +234,15 @@ cudaError_t launch_apply(bool fp32, bool weighted, const DevOp &op, const void *
 cudaError_t launch_prep_weighted(bool fp32, const DevOp &op, const void *W, int64_t S, void *cw_sorted,
                                  cudaStream_t st);
 
+// SummedPauliOp::square (k_square.cu): pair lists of the squared strings sq,
+// then out(A,K) (overwritten) from h (P,K); ws holds
+// square_workspace_bytes(P, A); *found -> device counter of the (i,j) pairs
+// whose product was found in sq (P^2 when every product is there).
+int64_t square_max_terms(int64_t P);
+size_t square_workspace_bytes(int64_t P, int64_t A);
+cudaError_t launch_square(bool fp32, const DevOp &op, const DevOp &sq, const void *h, int64_t K, void *out,
+                          void *ws, unsigned long long **found, cudaStream_t st);
+
 cudaError_t launch_sparse_repr(uint64_t x, uint64_t z, int ny, int n, uint64_t *cols, void *vals, cudaStream_t st);
 
 } // namespace fpg

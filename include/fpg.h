@@ -155,6 +155,20 @@ int fpg_summed_apply(const fpg_operator *op, const void *coeffs, int64_t n_opera
 int fpg_summed_apply_weighted(const fpg_operator *op, const void *coeffs, int64_t n_operators, const void *states,
                               const void *data, void *out, int64_t n_states, int32_t dtype, void *stream);
 
+/*
+ * Coefficients of the squares A_k^2 of a SummedPauliOp's operators
+ * A_k = sum_j coeffs(j,k) P_j:
+ *   out(a,k) = sum_{i,j: P_i P_j = phase * Q_a} phase * coeffs(i,k) * coeffs(j,k)
+ * over the strings Q_a of `sq` (normally all strings of weight up to
+ * min(n, 2 * max weight), calculate_pauli_strings_max_weight).  coeffs
+ * (n_strings(op), K) and out (n_strings(sq), K) are device arrays of dtype;
+ * out is OVERWRITTEN.  Returns FPG_ERR_INVALID if some product P_i P_j is not
+ * a string of sq.  Synchronises `stream` before returning.
+ * Replaces SummedPauliOp::square (__summed_pauli_op.hpp:197-268).
+ */
+int fpg_summed_square(const fpg_operator *op, const void *coeffs, int64_t n_operators, const fpg_operator *sq,
+                      void *out, int32_t dtype, void *stream);
+
 /* ------------------------------------------------------------------------
  * Batches: many expectation problems of uneven size (qubits, strings,
  * states, operators) run as one persistent work-queue launch per chunk class

@@ -70,6 +70,8 @@ def lib() -> ctypes.CDLL:
         L.fpo_summed_expectation.argtypes = [P, i64, ci, P, i64, i64, P, P]
         L.fpo_summed_apply.argtypes = [P, i64, ci, P, i64, i64, P, P]
         L.fpo_summed_apply_weighted.argtypes = [P, i64, ci, P, i64, i64, P, P, P]
+        L.fpo_summed_square.argtypes = [P, i64, ci, P, i64, P, i64, P]
+        L.fpo_summed_square.restype = ci
         L.fpo_max_threads.restype = ci
         _lib = L
     return _lib
@@ -231,6 +233,20 @@ def summed_apply_weighted(strings, h, psi, data) -> np.ndarray:
         _p(codes), len(strings), n, _p(h), h.shape[1], p2.shape[1], _p(p2), _p(d2), _p(out)
     )
     return out.reshape(psi.shape)
+
+
+def summed_square(strings, h, sq_strings) -> np.ndarray:
+    """Coefficients (A, K) of the squared operators over the strings
+    sq_strings (SummedPauliOp::square); raises if a product is missing."""
+    codes, n = codes_of(strings)
+    sq_codes, n2 = codes_of(sq_strings)
+    h = _c(h)
+    K = h.shape[1]
+    out = np.zeros((len(sq_strings), K), dtype=np.complex128)
+    rc = lib().fpo_summed_square(_p(codes), len(strings), n, _p(h), K, _p(sq_codes), len(sq_strings), _p(out))
+    if rc != 0:
+        raise ValueError("a product of two strings is not among the squared strings")
+    return out
 
 
 # --------------------------------------------------------------------------

@@ -313,6 +313,141 @@ void fpo_summed_apply_weighted(const uint8_t *codes, int64_t P, int n, const dou
     free(thr);
 }
 
+/*
+ * Product of two Pauli matrices (codes 0..3): result code a ^ b and the phase
+ * as a power of i -- the Pauli algebra XY = iZ, YZ = iX, ZX = iY (reversed
+ * order: -i), as tabulated by Pauli::operator* (__pauli.hpp:109-175).
+ */
+static const int k_pow_i[4][4] = {{0, 0, 0, 0}, {0, 0, 1, 3}, {0, 3, 0, 1}, {0, 1, 3, 0}};
+
+/* FNV-1a hash of a string of n codes (the reference keys a std::unordered_map
+ * by PauliString, __summed_pauli_op.hpp:209-213) */
+static uint64_t hash_codes(const uint8_t *c, int n)
+{
+    uint64_t hsh = 1469598103934665603ull;
+    for (int q = 0; q < n; ++q)
+        hsh = (hsh ^ c[q]) * 1099511628211ull;
+    return hsh;
+}
+
+/*
+ * fpo_summed_square <- SummedPauliOp::square (__summed_pauli_op.hpp:197-268),
+ * products as PauliString::operator* (__pauli_string.hpp:228-247).
+ * sq_codes: the A strings of the squared set (the caller passes
+ * calculate_pauli_strings_max_weight(n, min(n, 2 w))); out: (A, K) complex,
+ * overwritten.  Structure as the reference: an index map of the squared set
+ * (later duplicates overwrite earlier ones), the per-output pair lists
+ * t_aij built serially in (i, j) order, the coefficients transposed to (K, P),
+ * then out(a, k) += (phase * h(i, k)) * h(j, k) in parallel over (a, k).
+ * Returns 0, or -1 when a product is not in the set (the reference's map
+ * would then send it to index 0).
+ */
+int fpo_summed_square(const uint8_t *codes, int64_t P, int n, const double *h, int64_t K, const uint8_t *sq_codes,
+                      int64_t A, double *out)
+{
+    if (A <= 0 || K <= 0)
+        return 0;
+    memset(out, 0, (size_t)(A * K) * 2 * sizeof(double));
+    if (P <= 0)
+        return 0;
+    /* open-addressing index map */
+    int64_t cap = 1;
+    while (cap < 2 * A)
+        cap <<= 1;
+    int64_t *slot = (int64_t *)malloc((size_t)cap * sizeof(int64_t));
+    for (int64_t s = 0; s < cap; ++s)
+        slot[s] = -1;
+    for (int64_t a = 0; a < A; ++a)
+    {
+        int64_t s = (int64_t)(hash_codes(sq_codes + a * n, n) & (uint64_t)(cap - 1));
+        while (slot[s] >= 0 && memcmp(sq_codes + slot[s] * n, sq_codes + a * n, (size_t)n) != 0)
+            s = (s + 1) & (cap - 1);
+        slot[s] = a;
+    }
+    /* pair lists in CSR form: counts, then fill in (i, j) order */
+    int64_t *cnt = (int64_t *)calloc((size_t)A + 1, sizeof(int64_t));
+    int64_t *pidx = (int64_t *)malloc((size_t)(P * P) * sizeof(int64_t)); /* a of pair (i, j) */
+    int8_t *pph = (int8_t *)malloc((size_t)(P * P));                      /* phase power of i */
+    uint8_t *prod = (uint8_t *)malloc((size_t)n);
+    int missing = 0;
+    for (int64_t i = 0; i < P; ++i)
+        for (int64_t j = 0; j < P; ++j)
+        {
+            int e = 0;
+            for (int q = 0; q < n; ++q)
+            {
+                const uint8_t a = codes[i * n + q], b = codes[j * n + q];
+                e += k_pow_i[a][b];
+                prod[q] = (uint8_t)(a ^ b);
+            }
+            int64_t s = (int64_t)(hash_codes(prod, n) & (uint64_t)(cap - 1));
+            while (slot[s] >= 0 && memcmp(sq_codes + slot[s] * n, prod, (size_t)n) != 0)
+                s = (s + 1) & (cap - 1);
+            int64_t a = slot[s];
+            if (a < 0)
+            {
+                missing = 1;
+                a = 0;
+            }
+            pidx[i * P + j] = a;
+            pph[i * P + j] = (int8_t)(e & 3);
+            cnt[a + 1]++;
+        }
+    for (int64_t a = 0; a < A; ++a)
+        cnt[a + 1] += cnt[a];
+    int64_t *fill = (int64_t *)malloc((size_t)A * sizeof(int64_t));
+    memcpy(fill, cnt, (size_t)A * sizeof(int64_t));
+    int64_t *ti = (int64_t *)malloc((size_t)(P * P) * sizeof(int64_t));
+    int64_t *tj = (int64_t *)malloc((size_t)(P * P) * sizeof(int64_t));
+    int8_t *tp = (int8_t *)malloc((size_t)(P * P));
+    for (int64_t i = 0; i < P; ++i)
+        for (int64_t j = 0; j < P; ++j)
+        {
+            const int64_t a = pidx[i * P + j];
+            const int64_t x = fill[a]++;
+            ti[x] = i;
+            tj[x] = j;
+            tp[x] = pph[i * P + j];
+        }
+    /* coefficients transposed to (K, P) */
+    double *ht = (double *)malloc((size_t)(K * P) * 2 * sizeof(double));
+    for (int64_t i = 0; i < P; ++i)
+        for (int64_t k = 0; k < K; ++k)
+        {
+            ht[2 * (k * P + i)] = h[2 * (i * K + k)];
+            ht[2 * (k * P + i) + 1] = h[2 * (i * K + k) + 1];
+        }
+    static const double ph_re[4] = {1, 0, -1, 0}, ph_im[4] = {0, 1, 0, -1};
+#pragma omp parallel for schedule(dynamic) collapse(2)
+    for (int64_t a = 0; a < A; ++a)
+        for (int64_t k = 0; k < K; ++k)
+        {
+            double sr = 0, si = 0;
+            for (int64_t x = cnt[a]; x < cnt[a + 1]; ++x)
+            {
+                double ar, ai, br, bi;
+                const double *hi = ht + 2 * (k * P + ti[x]), *hj = ht + 2 * (k * P + tj[x]);
+                cmul(ph_re[tp[x]], ph_im[tp[x]], hi[0], hi[1], &ar, &ai);
+                cmul(ar, ai, hj[0], hj[1], &br, &bi);
+                sr += br;
+                si += bi;
+            }
+            out[2 * (a * K + k)] = sr;
+            out[2 * (a * K + k) + 1] = si;
+        }
+    free(ht);
+    free(tp);
+    free(tj);
+    free(ti);
+    free(fill);
+    free(prod);
+    free(pph);
+    free(pidx);
+    free(cnt);
+    free(slot);
+    return missing ? -1 : 0;
+}
+
 int fpo_max_threads(void)
 {
     return max_threads();

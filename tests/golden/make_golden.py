@@ -113,6 +113,16 @@ def main() -> None:
         os.path.join(HERE, "summed_square.npz"),
         strings=_s(strings), h=h, sq_strings=_s(sq_strings), sq_h=sq_h,
     )
+    # weight <= 2 strings at n = 6 (identity included), K = 3: 154 strings,
+    # 1909 squared strings (weight <= 4)
+    rng = np.random.default_rng(8)
+    strings = ref.pauli_strings_max_weight(6, 2)
+    h = rng.standard_normal((len(strings), 3)) + 1j * rng.standard_normal((len(strings), 3))
+    sq_strings, sq_h = ref.summed_square(strings, h)
+    np.savez_compressed(
+        os.path.join(HERE, "summed_square_n6.npz"),
+        strings=_s(strings), h=h, sq_strings=_s(sq_strings), sq_h=sq_h,
+    )
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -348,6 +348,50 @@ def test_tensor_core_weighted_coefficients():
     assert normwise(got.cpu().numpy(), want) < TOL_MIXED
 
 
+# ------------------------------------------------------------ square
+
+
+@pytest.mark.parametrize("name", ["summed_square.npz", "summed_square_n6.npz"])
+def test_summed_square_vs_reference(name):
+    g = golden(name)
+    op = fp.SummedPauliOp(_strs(g["strings"]), g["h"])
+    sq = op.square()
+    assert sq.pauli_strings_as_str == _strs(g["sq_strings"])
+    assert normwise(sq.coeffs.T, g["sq_h"]) < TOL_C128
+
+
+@pytest.mark.parametrize("n,w,K,dup", [(5, 2, 4, False), (8, 2, 9, False), (7, 1, 3, True), (4, 4, 2, False)])
+def test_summed_square_vs_oracle(n, w, K, dup):
+    torch = pytest.importorskip("torch")
+    from fast_pauli import _abi
+
+    L = _abi.lib()
+    rng = np.random.default_rng(40 + n + w)
+    strings = oracle.calculate_pauli_strings_max_weight(n, w)
+    if dup:  # repeated strings: their products with each other are the identity
+        strings = strings + strings[3:9]
+    rng.shuffle(strings)
+    P = len(strings)
+    h = rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))
+    sq_strings = oracle.calculate_pauli_strings_max_weight(n, min(n, 2 * w))
+    want = oracle.summed_square(strings, h, sq_strings)
+    op, q = _abi.Operator(strings), _abi.Operator(sq_strings)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for dtype, tdt, tol in ((_abi.FPG_C128, torch.complex128, TOL_C128), (_abi.FPG_C64, torch.complex64, TOL_MIXED)):
+        dh = torch.from_numpy(h).to(tdt).cuda()
+        out = torch.full((len(sq_strings), K), 7.0, dtype=tdt, device="cuda")  # overwritten
+        _abi.check(L.fpg_summed_square(op.handle, dh.data_ptr(), K, q.handle, out.data_ptr(), dtype, st))
+        assert normwise(out.cpu().numpy(), want) < tol, dtype
+    # a squared set that misses products is an argument error, reported after the run
+    small = _abi.Operator(sq_strings[: len(sq_strings) // 2])
+    out = torch.zeros((len(sq_strings) // 2, K), dtype=torch.complex128, device="cuda")
+    dh = torch.from_numpy(h).cuda()
+    rc = L.fpg_summed_square(op.handle, dh.data_ptr(), K, small.handle, out.data_ptr(), _abi.FPG_C128, st)
+    assert rc == _abi.FPG_ERR_INVALID
+    for o in (op, q, small):
+        o.close()
+
+
 # ------------------------------------------------------------ raw C ABI
 
 

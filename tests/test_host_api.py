@@ -184,14 +184,6 @@ def test_summed_pauli_op_host_side():
         fp.SummedPauliOp(["XX", "YY"], np.ones((3, 1)))
 
 
-def test_summed_square_golden():
-    g = golden("summed_square.npz")
-    op = fp.SummedPauliOp([str(s) for s in g["strings"]], g["h"])
-    sq = op.square()
-    assert sq.pauli_strings_as_str == [str(s) for s in g["sq_strings"]]
-    np.testing.assert_allclose(sq.coeffs.T, g["sq_h"], atol=1e-14)
-
-
 def test_helpers_match_oracle_and_golden():
     g = golden("helpers.npz")
     for key in g.files:

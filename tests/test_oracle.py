@@ -73,6 +73,22 @@ def test_small_methods_golden():
         assert normwise(v, g[k]) < 1e-14, k
 
 
+@pytest.mark.parametrize("name", ["summed_square.npz", "summed_square_n6.npz"])
+def test_summed_square_golden(name):
+    g = golden(name)
+    got = oracle.summed_square([str(x) for x in g["strings"]], g["h"], [str(x) for x in g["sq_strings"]])
+    assert normwise(got, g["sq_h"]) < 1e-14
+    # the squared set is the helper's max-weight set
+    n = len(str(g["strings"][0]))
+    w = max(sum(c != "I" for c in str(x)) for x in g["strings"])
+    assert [str(x) for x in g["sq_strings"]] == oracle.calculate_pauli_strings_max_weight(n, min(n, 2 * w))
+
+
+def test_summed_square_missing_product_is_reported():
+    with pytest.raises(ValueError):
+        oracle.summed_square(["XI", "IZ"], np.ones((2, 1)), ["II", "XI", "IZ"])  # XZ missing
+
+
 def test_config2_reduced_golden():
     g = golden("config2_reduced_summed_expectation.npz")
     got = oracle.summed_expectation([str(x) for x in g["strings"]], g["h"], g["states"])
