@@ -249,10 +249,13 @@ def run_ours(args, rank, world, dist):
         "kernel": "expectation stage (fpg_expect_strings: k_expect_pair + k_expect_marg + k_expect_wht)",
         "kernel_ms": t_expect * 1e3,
         "algorithmic_bytes_per_launch": alg_bytes_expect,
-        "pipe": {"kind": "fp64", "ops_per_launch": fp64_ops, "achieved_tflops": 2 * fp64_ops / t_expect / 1e12,
-                 "peak_tflops": FP64_PEAK_TFLOPS,
-                 "frac": 2 * fp64_ops / t_expect / 1e12 / FP64_PEAK_TFLOPS,
-                 "note": "FMA-equivalent float64 instructions x2; FP64 pipe bound"},
+        "pipe": {"kind": "fp64-equivalent", "ops_per_launch": fp64_ops,
+                 "achieved_tflops": 2 * fp64_ops / t_expect / 1e12,
+                 "fp64_pipe_peak_tflops": FP64_PEAK_TFLOPS,
+                 "vs_fp64_pipe": 2 * fp64_ops / t_expect / 1e12 / FP64_PEAK_TFLOPS,
+                 "note": "the stage's float64 operations (FMA-equivalent x2) per second, against the measured float64 "
+                         "pipe; above 1 because the kernels run the float64 arithmetic as double-float on the "
+                         "float32 pipes"},
     }
 
     # ---- end to end through the public API, host (pinned) buffers ---------
@@ -660,9 +663,10 @@ def run_serve(args):
         reqs.append(dict(n=n, P=P, S=S, K=K, kind=kind, op=_abi.Operator(strings), psi=psi, h=h, data=data,
                          out=torch.empty(out_shape, dtype=torch.complex64, device="cuda")))
     torch.cuda.synchronize()
-    gaps = rng.exponential(1.0 / args.rate, size=n_req)
+    unit_gaps = rng.exponential(1.0, size=n_req)  # scaled by 1/rate per run
 
-    def serve(n_slots):
+    def serve(n_slots, rate):
+        gaps = unit_gaps / rate
         srv = _abi.Server(_abi.FPG_C64, n_slots=n_slots, hbm_budget_bytes=args.budget_gb << 30)
         # warm-up: one small request
         r0 = min(reqs, key=lambda r: r["P"] << r["n"])
@@ -685,23 +689,45 @@ def run_serve(args):
         return lat, wall, st
 
     terms = sum(r["P"] * (1 << r["n"]) * r["S"] for r in reqs)
+    rates = [float(x) for x in args.rates.split(",")]
+    ns = np.array([r["n"] for r in reqs])
+    # service time of every request alone (one slot, one at a time): the floor
+    # under any latency
+    alone = []
+    srv = _abi.Server(_abi.FPG_C64, n_slots=1, hbm_budget_bytes=args.budget_gb << 30)
+    for r in reqs:
+        info = srv.wait(srv.submit(r["kind"], r["op"], r["h"].data_ptr(), r["K"], r["psi"].data_ptr(),
+                                   r["out"].data_ptr(), r["S"], r["data"].data_ptr()))
+        alone.append((info["done_us"] - info["start_us"]) / 1e3)
+    srv.close()
+    alone = np.array(alone)
+    le20 = ns <= 20
     out = {"metric": "serving latency ms / amplitude-terms/s",
-           "workload": f"config 5: {n_req} requests, Poisson rate {args.rate}/s, n~U{{10..{args.max_n}}}, "
+           "workload": f"config 5: {n_req} requests per rate, Poisson rates {rates}/s, n~U{{10..{args.max_n}}}, "
                        "P log-uniform 32..2048 uniform strings, S~U{1..64}, K log-uniform 1..64, "
-                       "50/50 expectation_value / apply_weighted, complex64"}
-    for name, slots in (("served", args.slots), ("plain_per_request", 1)):
-        lat, wall, st = serve(slots)
-        buckets = {}
-        ns = np.array([r["n"] for r in reqs])
-        for lo, hi in ((10, 14), (15, 20), (21, 24)):
-            m = (ns >= lo) & (ns <= hi)
-            if m.any():
-                buckets[f"n{lo}-{hi}"] = {"count": int(m.sum()), "p50_ms": float(np.percentile(lat[m], 50)),
-                                          "p99_ms": float(np.percentile(lat[m], 99))}
-        out[name] = {"slots": slots, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                     "throughput_terms_per_s": terms / wall, "requests_per_s": n_req / wall, "wall_s": wall,
-                     "by_n": buckets, "peak_running": st["peak_running"],
-                     "peak_reserved_gb": st["peak_reserved_bytes"] / 2**30}
+                       "50/50 expectation_value / apply_weighted, complex64",
+           "service_alone_ms": {"p50": float(np.percentile(alone, 50)), "p99": float(np.percentile(alone, 99)),
+                                "p99_n_le_20": float(np.percentile(alone[le20], 99)),
+                                "sum_s": float(alone.sum()) / 1e3},
+           "capacity_requests_per_s": n_req / (float(alone.sum()) / 1e3),
+           "sweep": []}
+    for rate in rates:
+        row = {"rate_per_s": rate}
+        for name, slots in (("served", args.slots), ("plain_per_request", 1)):
+            lat, wall, st = serve(slots, rate)
+            buckets = {}
+            for lo, hi in ((10, 14), (15, 20), (21, 24)):
+                m = (ns >= lo) & (ns <= hi)
+                if m.any():
+                    buckets[f"n{lo}-{hi}"] = {"count": int(m.sum()), "p50_ms": float(np.percentile(lat[m], 50)),
+                                              "p99_ms": float(np.percentile(lat[m], 99))}
+            row[name] = {"slots": slots, "p50_ms": float(np.percentile(lat, 50)),
+                         "p99_ms": float(np.percentile(lat, 99)),
+                         "p99_ms_n_le_20": float(np.percentile(lat[le20], 99)),
+                         "throughput_terms_per_s": terms / wall, "requests_per_s": n_req / wall, "wall_s": wall,
+                         "by_n": buckets, "peak_running": st["peak_running"],
+                         "peak_reserved_gb": st["peak_reserved_bytes"] / 2**30}
+        out["sweep"].append(row)
     return out
 
 
@@ -721,8 +747,8 @@ def main():
     ap.add_argument("--workload", default="summed", choices=["summed", "batch", "serve", "square"],
                     help="summed: configuration 2 (default line); batch: configuration 4; serve: configuration 5; "
                          "square: SummedPauliOp.square of the configuration-2 operators")
-    ap.add_argument("--requests", type=int, default=200, help="serve: number of requests")
-    ap.add_argument("--rate", type=float, default=50.0, help="serve: Poisson arrival rate (requests/s)")
+    ap.add_argument("--requests", type=int, default=60, help="serve: requests per rate")
+    ap.add_argument("--rates", default="2,4,8", help="serve: Poisson arrival rates to sweep (requests/s)")
     ap.add_argument("--max-n", type=int, default=24, help="serve: largest qubit count")
     ap.add_argument("--slots", type=int, default=8, help="serve: concurrent request slots")
     ap.add_argument("--budget-gb", type=int, default=64, help="serve: HBM budget for request scratch")

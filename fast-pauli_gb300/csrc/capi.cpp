@@ -424,9 +424,26 @@ int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int6
     const ExpectPlan plan = plan_expect(op, S, fp32, psi);
     int64_t off[kNumFam];
     const int64_t scratch = family_partials(op, plan, S, off);
+    // scratch: the df64 range flag of the float64 path (see df64.cuh) and the
+    // families' partial tables
+    const bool need_flag = !fp32 && (!op->pairs.empty() || !op->margs.empty() || !op->wht.empty());
+    const size_t flag_bytes = need_flag ? 256 : 0;
     Scratch partial(st);
-    if (scratch > 0)
-        FPG_CUDA(partial.alloc((size_t)scratch * sizeof(double)));
+    if (scratch > 0 || need_flag)
+        FPG_CUDA(partial.alloc(flag_bytes + (size_t)scratch * sizeof(double)));
+    int *range_flag = need_flag ? (int *)partial.p : nullptr;
+    if (need_flag)
+        FPG_CUDA(cudaMemsetAsync(range_flag, 0, sizeof(int), st));
+    double *partials = (double *)((char *)partial.p + flag_bytes);
+    // float64 path: the state split into df64 once (same size), when it fits
+    Scratch split(st);
+    const int64_t n_elem = ((int64_t)1 << op->n) * S;
+    if (need_flag && n_elem * 16 <= kDfSplitMaxBytes)
+    {
+        FPG_CUDA(split.alloc((size_t)n_elem * 16));
+        FPG_CUDA(launch_df_split(psi, n_elem, split.p, range_flag, st));
+    }
+    const void *psi_df = split.p;
     // family f writes ev directly (caller order) or its own partial table
     // (family-local order, reduced below)
     auto target = [&](int f, DevOp &d, ExpectPlan &pl) -> double * {
@@ -437,7 +454,7 @@ int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int6
             return ev;
         d.orig = op->d_local;
         d.P = op->fam_begin[f + 1] - op->fam_begin[f];
-        return (double *)partial.p + off[f];
+        return partials + off[f];
     };
     DevOp d;
     ExpectPlan pl;
@@ -445,18 +462,19 @@ int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int6
     {
         double *dst = target(kFamWht, d, pl);
         FPG_CUDA(launch_expect_wht(fp32, psi, S, op->n, d, op->d_wht, (int)op->wht.size(), op->wht_max_count,
-                                   pl.wht_TC, pl.wht_ctiles, pl.n_splits, dst, st));
+                                   pl.wht_TC, pl.wht_ctiles, pl.n_splits, dst, range_flag, psi_df, st));
     }
     if (!op->margs.empty())
     {
         double *dst = target(kFamMarg, d, pl);
         FPG_CUDA(launch_expect_marg(fp32, psi, S, op->n, d, op->d_margs, (int)op->margs.size(), op->marg_max_high,
-                                    pl.wht_TC, pl.wht_ctiles, pl.n_splits, dst, st));
+                                    pl.wht_TC, pl.wht_ctiles, pl.n_splits, dst, range_flag, psi_df, st));
     }
     if (!op->pairs.empty())
     {
         double *dst = target(kFamPair, d, pl);
-        FPG_CUDA(launch_expect_pair(fp32, psi, S, op->n, d, op->d_pairs, (int)op->pairs.size(), pl, dst, st));
+        FPG_CUDA(launch_expect_pair(fp32, psi, S, op->n, d, op->d_pairs, (int)op->pairs.size(), pl, dst, range_flag,
+                                    psi_df, st));
     }
     {
         double *dst = target(kFamDirect, d, pl);
@@ -469,7 +487,7 @@ int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int6
     }
     for (int f = 0; f < kNumFam; ++f)
         if (off[f] >= 0)
-            FPG_CUDA(launch_reduce_family((const double *)partial.p + off[f], plan.fam_splits[f],
+            FPG_CUDA(launch_reduce_family(partials + off[f], plan.fam_splits[f],
                                           op->fam_begin[f + 1] - op->fam_begin[f], S, op->d_glob + op->fam_begin[f],
                                           ev, st));
     return FPG_OK;
@@ -494,7 +512,10 @@ size_t request_scratch_bytes(const fpg_operator *op, int64_t K, int64_t S, bool 
     }
     const ExpectPlan plan = plan_expect(op, S, fp32, nullptr);
     int64_t off[kNumFam];
-    size_t b = P * (size_t)S * sizeof(double) + (size_t)family_partials(op, plan, S, off) * sizeof(double);
+    size_t b = P * (size_t)S * sizeof(double) + (size_t)family_partials(op, plan, S, off) * sizeof(double) + 512;
+    const int64_t split_bytes = ((int64_t)1 << op->n) * S * 16;
+    if (!fp32 && (!op->pairs.empty() || !op->margs.empty() || !op->wht.empty()) && split_bytes <= kDfSplitMaxBytes)
+        b += (size_t)split_bytes; // the df64 copy of the state
     if (fp32)
         b += tc_workspace_bytes(2 * K, S, op->P);
     return b + 4096;
@@ -755,8 +776,10 @@ extern "C"
             return set_error(FPG_ERR_CUDA, "cannot select the operator's device");
         cudaStream_t st = (cudaStream_t)stream;
         const bool fp32 = dtype == FPG_C64;
+        // per-string table, then (float64) the contraction's df64 range flag
         Scratch evb(st);
-        FPG_CUDA(evb.alloc((size_t)op->P * (size_t)n_states * sizeof(double)));
+        const size_t ev_bytes = ((size_t)op->P * (size_t)n_states * sizeof(double) + 255) & ~(size_t)255;
+        FPG_CUDA(evb.alloc(ev_bytes + 256));
         if (int rc = run_expect_strings(op, states, (double *)evb.p, n_states, fp32, st))
             return rc;
         if (fp32)
@@ -768,8 +791,10 @@ extern "C"
                                                ws.p, st));
             return FPG_OK;
         }
+        int *range_flag = (int *)((char *)evb.p + ev_bytes);
+        FPG_CUDA(cudaMemsetAsync(range_flag, 0, sizeof(int), st));
         FPG_CUDA(launch_contract_real(fp32, coeffs, fp32, (const double *)evb.p, op->P, n_operators, n_states, out,
-                                      st));
+                                      range_flag, st));
         return FPG_OK;
     }
 

@@ -181,27 +181,47 @@ cudaError_t launch_reduce_family(const double *partial, int n_splits, int64_t Pf
                                  double *ev, cudaStream_t st);
 
 // Pair kernel over pair chunks; uses plan.TC / V / n_ctiles / n_splits like the
-// direct kernel and writes like it.
+// direct kernel and writes like it.  complex128 states run in df64 on the
+// float32 pipes (df64.cuh) followed by the float64 form, which recomputes
+// only when *range_flag (a device int, zero before the call) was raised;
+// psi_df = the state split by launch_df_split (which raises the flag), or
+// null to split inside the kernel (which raises it).  complex64 states
+// ignore range_flag and psi_df.
 cudaError_t launch_expect_pair(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const PairChunk *d_chunks,
-                               int n_chunks, const ExpectPlan &plan, double *out, cudaStream_t st);
+                               int n_chunks, const ExpectPlan &plan, double *out, int *range_flag,
+                               const void *psi_df, cudaStream_t st);
 
 // Marginal kernel over marginal chunks: one complex element per lane, TC
 // column lanes (the V = 1 tiling, plan.wht_TC / wht_ctiles), 256 threads;
 // max_high_bits = the largest number of zmask bits >= 5 over the chunks.
+// range_flag and psi_df as launch_expect_pair.
 cudaError_t launch_expect_marg(bool fp32, const void *psi, int64_t S, int n, const DevOp &op,
                                const MargChunk *d_chunks, int n_chunks, int max_high_bits, int TC, int n_ctiles,
-                               int n_splits, double *out, cudaStream_t st);
+                               int n_splits, double *out, int *range_flag, const void *psi_df, cudaStream_t st);
+
+// out[i] = complex128 psi[i] as df64 (re_h, re_l, im_h, im_l) floats, i <
+// count; raises *range_flag for values outside the df64 range.
+cudaError_t launch_df_split(const void *psi, int64_t count, void *out, int *range_flag, cudaStream_t st);
+// State size up to which the float64 path splits the state into a scratch
+// copy once per call instead of inside every kernel.
+constexpr int64_t kDfSplitMaxBytes = int64_t(16) << 30;
 
 // Transform kernel over WHT chunks (128 threads = TC column lanes x 128/TC row
 // lanes, one complex element per lane); writes like launch_expect_chunks.
+// complex128: df64 on psi_df then the float64 recomputation gated by
+// *range_flag, or float64 alone when psi_df is null.
 cudaError_t launch_expect_wht(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const WhtChunk *d_chunks,
                               int n_chunks, int max_count, int TC, int n_ctiles, int n_splits, double *out,
-                              cudaStream_t st);
+                              int *range_flag, const void *psi_df, cudaStream_t st);
 
 // out(K,S) += H^T(K,P) * E(P,S); H complex (P,K), E real float64 (P,S).
 // out complex128 (fp32=false) or complex64 (fp32=true).
+// range_flag (complex128 H and out only; a device int, zero before the call):
+// when given, the GEMM runs in df64 on the float32 pipes, or in float64 when
+// some value of H or E lies outside the df64 range (df64.cuh); when null,
+// float64 throughout.
 cudaError_t launch_contract_real(bool out_c64, const void *H, bool h_c64, const double *E, int64_t P, int64_t K,
-                                 int64_t S, void *out, cudaStream_t st);
+                                 int64_t S, void *out, int *range_flag, cudaStream_t st);
 
 // Tensor-core (tcgen05, 3xTF32, float32 accumulation) forms for the mixed
 // path; ws must hold tc_workspace_bytes(M, N, Kd) of the GEMM they run:

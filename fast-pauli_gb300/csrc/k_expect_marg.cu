@@ -13,14 +13,20 @@
 // sum per string.  Per 32-row block the marginals of the five low bits come
 // from a small tree (4-row groups: pair sums, then group sums), ~2.1 adds per
 // row and part; the block total is added to the marginal of each higher bit
-// set in the block's base.  Per row that is q (4 operations) plus ~4.3 adds
-// for both parts, against ~14 for the 16-point transform kernel.
+// set in the block's base.
 //
 // Rows: as k_expect_pair.cu -- blocks paired for x >= 32, rows paired inside
 // a block for 0 < x < 32 (16 rows visited), all rows for x = 0.  Layout: TC
 // column lanes x (256 / TC) row lanes, one complex element per lane; grid
-// (chunks, row splits, column tiles).  float32 path: block sums in float32,
-// Kahan-compensated across blocks; float64 across threads.
+// (chunks, row splits, column tiles).
+//
+// Arithmetic (the policy A):
+//  * complex64 states: float32 sums inside a block, Kahan-compensated float32
+//    across blocks, float64 across threads;
+//  * complex128 states: double-float (df64.cuh) throughout the block and
+//    across blocks -- the float64 result to ~2^-46 of sum |terms| at float32
+//    pipe rates -- and float64 across threads.
+#include "df64.cuh"
 #include "expect_body.cuh"
 
 namespace fpg
@@ -28,108 +34,276 @@ namespace fpg
 namespace
 {
 
-template <typename T> __device__ __forceinline__ void kadd(T &acc, T &cmp, T x)
+struct DF
 {
-    if constexpr (sizeof(T) == 8)
-    {
-        acc += x;
-    }
-    else
-    {
-        const T y = x - cmp;
-        const T s = acc + y;
-        cmp = (s - acc) - y;
-        acc = s;
-    }
-}
-
-template <typename T> struct Cplx;
-template <> struct Cplx<double>
-{
-    using type = double2;
+    float h, l;
 };
-template <> struct Cplx<float>
+
+// complex64 states: float values, Kahan accumulators
+struct ArF32
 {
-    using type = float2;
+    using in_t = float;
+    static constexpr bool kRaises = false, kRecompute = false;
+    using val = float;
+    struct acc
+    {
+        float v, c;
+    };
+    static __device__ __forceinline__ val zero()
+    {
+        return 0.f;
+    }
+    static __device__ __forceinline__ void add(val &a, val b)
+    {
+        a += b;
+    }
+    static __device__ __forceinline__ val sum(val a, val b)
+    {
+        return a + b;
+    }
+    static __device__ __forceinline__ acc acc_zero()
+    {
+        return acc{0.f, 0.f};
+    }
+    static __device__ __forceinline__ void acc_add(acc &a, val x)
+    {
+        const float y = x - a.c;
+        const float s = a.v + y;
+        a.c = (s - a.v) - y;
+        a.v = s;
+    }
+    static __device__ __forceinline__ double to_double(const acc &a)
+    {
+        return (double)a.v - (double)a.c;
+    }
+    static __device__ __forceinline__ acc from2(float2 f)
+    {
+        return acc{f.x, f.y};
+    }
+    static __device__ __forceinline__ float2 to2(const acc &a)
+    {
+        return make_float2(a.v, a.c);
+    }
+    // q = conj(psi_a) psi_b at element pointers pa, pb
+    static __device__ __forceinline__ void q(const in_t *psi, int64_t ea, int64_t eb, bool re, bool im, val &vr,
+                                             val &vi, bool &)
+    {
+        const float2 a = __ldg(reinterpret_cast<const float2 *>(psi) + ea);
+        const float2 b = __ldg(reinterpret_cast<const float2 *>(psi) + eb);
+        if (re)
+            vr = fmaf(a.x, b.x, a.y * b.y);
+        if (im)
+            vi = fmaf(a.x, b.y, -(a.y * b.x));
+    }
+};
+
+// complex128 states, float64 arithmetic: the recomputation for inputs
+// outside the df64 range
+struct ArF64
+{
+    using in_t = double;
+    static constexpr bool kRaises = false, kRecompute = true;
+    using val = double;
+    using acc = double;
+    static __device__ __forceinline__ val zero()
+    {
+        return 0.0;
+    }
+    static __device__ __forceinline__ void add(val &a, val b)
+    {
+        a += b;
+    }
+    static __device__ __forceinline__ val sum(val a, val b)
+    {
+        return a + b;
+    }
+    static __device__ __forceinline__ acc acc_zero()
+    {
+        return 0.0;
+    }
+    static __device__ __forceinline__ void acc_add(acc &a, val x)
+    {
+        a += x;
+    }
+    static __device__ __forceinline__ double to_double(const acc &a)
+    {
+        return a;
+    }
+    static __device__ __forceinline__ acc from2(float2 f)
+    {
+        return (double)__hiloint2double(__float_as_int(f.y), __float_as_int(f.x));
+    }
+    static __device__ __forceinline__ float2 to2(const acc &a)
+    {
+        return make_float2(__int_as_float(__double2loint(a)), __int_as_float(__double2hiint(a)));
+    }
+    static __device__ __forceinline__ void q(const in_t *psi, int64_t ea, int64_t eb, bool re, bool im, val &vr,
+                                             val &vi, bool &)
+    {
+        const double2 a = __ldg(reinterpret_cast<const double2 *>(psi) + ea);
+        const double2 b = __ldg(reinterpret_cast<const double2 *>(psi) + eb);
+        if (re)
+            vr = fma(a.x, b.x, a.y * b.y);
+        if (im)
+            vi = fma(a.x, b.y, -(a.y * b.x));
+    }
+};
+
+// complex128 states: df64 values and accumulators; raises the range flag
+struct ArDF
+{
+    using in_t = double;
+    static constexpr bool kRaises = true, kRecompute = false;
+    using val = DF;
+    using acc = DF;
+    static __device__ __forceinline__ val zero()
+    {
+        return DF{0.f, 0.f};
+    }
+    static __device__ __forceinline__ void add(val &a, val b)
+    {
+        df_add(a.h, a.l, b.h, b.l);
+    }
+    static __device__ __forceinline__ val sum(val a, val b)
+    {
+        df_add(a.h, a.l, b.h, b.l);
+        return a;
+    }
+    static __device__ __forceinline__ acc acc_zero()
+    {
+        return DF{0.f, 0.f};
+    }
+    static __device__ __forceinline__ void acc_add(acc &a, val x)
+    {
+        df_add(a.h, a.l, x.h, x.l);
+    }
+    static __device__ __forceinline__ double to_double(const acc &a)
+    {
+        return df_to_double(a.h, a.l);
+    }
+    static __device__ __forceinline__ acc from2(float2 f)
+    {
+        return DF{f.x, f.y};
+    }
+    static __device__ __forceinline__ float2 to2(const acc &a)
+    {
+        return make_float2(a.h, a.l);
+    }
+    static __device__ __forceinline__ void q(const in_t *psi, int64_t ea, int64_t eb, bool re, bool im, val &vr,
+                                             val &vi, bool &bad)
+    {
+        const float4 a = split_complex(__ldg(reinterpret_cast<const uint4 *>(psi) + ea), bad);
+        const float4 b = split_complex(__ldg(reinterpret_cast<const uint4 *>(psi) + eb), bad);
+        qdf(a, b, re, im, vr, vi);
+    }
+    // q = conj(a) b from df64 amplitudes (re_h, re_l, im_h, im_l)
+    static __device__ __forceinline__ void qdf(float4 a, float4 b, bool re, bool im, val &vr, val &vi)
+    {
+        if (re)
+        {
+            vr = DF{0.f, 0.f};
+            df_fma(a.x, a.y, b.x, b.y, vr.h, vr.l);
+            df_fma(a.z, a.w, b.z, b.w, vr.h, vr.l);
+        }
+        if (im)
+        {
+            vi = DF{0.f, 0.f};
+            df_fma(a.x, a.y, b.z, b.w, vi.h, vi.l);
+            df_fma(-a.z, -a.w, b.x, b.y, vi.h, vi.l);
+        }
+    }
+};
+
+// complex128 states already split into df64 (k_df_split, which also checked
+// the range): the arithmetic of ArDF without the split
+struct ArDFS : ArDF
+{
+    using in_t = float4;
+    static constexpr bool kRaises = false, kRecompute = false;
+    static __device__ __forceinline__ void q(const in_t *psi, int64_t ea, int64_t eb, bool re, bool im, val &vr,
+                                             val &vi, bool &)
+    {
+        qdf(__ldg(psi + ea), __ldg(psi + eb), re, im, vr, vi);
+    }
 };
 
 // Sums of one block: bt[part] (total) and bl[part][j] (rows whose visited-row
 // bit j is set).  LB = 5: all 32 rows, visited bit j = row bit j.  LB = 4:
 // the 16 rows with bit pl clear; visited bit j = row bit (j < pl ? j : j + 1).
-template <typename T, int LB>
-__device__ __forceinline__ void block_marginals(const T *__restrict__ psi, int64_t S, int64_t t0, uint64_t base,
-                                                uint64_t baseB, uint32_t xl, int pl, int RB, bool need_re,
-                                                bool need_im, T (&bt)[2], T (&bl)[2][5])
+template <typename A, int LB>
+__device__ __forceinline__ void block_marginals(const typename A::in_t *__restrict__ psi, int64_t S, int64_t t0,
+                                                uint64_t base, uint64_t baseB, uint32_t xl, int pl, int RB,
+                                                bool need_re, bool need_im, typename A::val (&bt)[2],
+                                                typename A::val (&bl)[2][5], bool &bad)
 {
-    using CT = typename Cplx<T>::type;
-    const CT *ps = reinterpret_cast<const CT *>(psi);
+    using val = typename A::val;
     // 16 visited rows at a time (LB = 5: two halves, bit 4 from the half)
 #pragma unroll 1
     for (int h = 0; h < (1 << (LB - 4)); ++h)
     {
-        T hs[2] = {T(0), T(0)};
+        val hs[2] = {A::zero(), A::zero()};
 #pragma unroll
         for (int k = 0; k < 4; ++k)
         {
-            T v[4][2];
+            val v[4][2];
 #pragma unroll
             for (int u = 0; u < 4; ++u)
             {
                 const uint32_t m2 = (uint32_t)(16 * h + 4 * k + u);
                 const uint32_t r = LB == 5 ? m2 : (((m2 >> pl) << (pl + 1)) | (m2 & ((1u << pl) - 1u)));
-                v[u][0] = T(0);
-                v[u][1] = T(0);
+                v[u][0] = A::zero();
+                v[u][1] = A::zero();
                 if ((int)r < RB)
-                {
-                    const CT a = __ldg(ps + (int64_t)(base + r) * S + t0);
-                    const CT b = __ldg(ps + (int64_t)(baseB + (uint64_t)(r ^ xl)) * S + t0);
-                    if (need_re)
-                        v[u][0] = fma(a.x, b.x, a.y * b.y);
-                    if (need_im)
-                        v[u][1] = fma(a.x, b.y, -(a.y * b.x));
-                }
+                    A::q(psi, (int64_t)(base + r) * S + t0, (int64_t)(baseB + (r ^ xl)) * S + t0, need_re, need_im,
+                         v[u][0], v[u][1], bad);
             }
 #pragma unroll
             for (int p = 0; p < 2; ++p)
             {
                 if (p == 0 ? !need_re : !need_im)
                     continue;
-                const T p0 = v[0][p] + v[1][p];
-                const T p1 = v[2][p] + v[3][p];
-                bl[p][0] += v[1][p];
-                bl[p][0] += v[3][p];
-                bl[p][1] += p1;
-                const T g = p0 + p1;
-                hs[p] += g;
+                const val p0 = A::sum(v[0][p], v[1][p]);
+                const val p1 = A::sum(v[2][p], v[3][p]);
+                A::add(bl[p][0], v[1][p]);
+                A::add(bl[p][0], v[3][p]);
+                A::add(bl[p][1], p1);
+                const val g = A::sum(p0, p1);
+                A::add(hs[p], g);
                 if (k & 1)
-                    bl[p][2] += g;
+                    A::add(bl[p][2], g);
                 if (k & 2)
-                    bl[p][3] += g;
+                    A::add(bl[p][3], g);
             }
         }
 #pragma unroll
         for (int p = 0; p < 2; ++p)
         {
-            bt[p] += hs[p];
+            A::add(bt[p], hs[p]);
             if (h)
-                bl[p][4] += hs[p];
+                A::add(bl[p][4], hs[p]);
         }
     }
 }
 
-template <typename T> constexpr int kMargMinBlocks = 2;
-
-template <typename T, int NH>
-__global__ void __launch_bounds__(256, kMargMinBlocks<T>)
-    k_expect_marg(const T *__restrict__ psi, int64_t S, int n, const StringRec *__restrict__ recs,
+// range_flag: ArDF raises it for inputs outside the df64 range; ArF64 (the
+// recomputation launched after it) returns at once unless it is set.
+template <typename A, int NH>
+__global__ void __launch_bounds__(256, 2)
+    k_expect_marg(const typename A::in_t *__restrict__ psi, int64_t S, int n, const StringRec *__restrict__ recs,
                   const int32_t *__restrict__ orig, int64_t P, const MargChunk *__restrict__ chunks, int TC,
-                  int n_splits, double *__restrict__ out)
+                  int n_splits, double *__restrict__ out, int *__restrict__ range_flag)
 {
+    if (A::kRecompute && *range_flag == 0)
+        return;
+    bool bad = false;
+    using val = typename A::val;
+    using acc = typename A::acc;
     constexpr int NV = 2 * (1 + 5 + NH); // values per thread: [part][total, low 5, high NH]
     constexpr int NVB = 8;               // values reduced per pass
     extern __shared__ double smem[];
     double *red = smem;                  // [NVB][256]
     double *res = smem + NVB * 256;      // [NV][TC] totals per column lane
+    float2 *smh = reinterpret_cast<float2 *>(res + NV * TC); // [2][NH][256] high-bit accumulators
 
     const MargChunk ch = chunks[blockIdx.x];
     const int tid = threadIdx.x;
@@ -153,30 +327,21 @@ __global__ void __launch_bounds__(256, kMargMinBlocks<T>)
     const int64_t b1 = min(nblk, b0 + per);
     const bool need_re = (ch.flags & 1) != 0, need_im = (ch.flags & 2) != 0;
 
-    // row bits >= 5 used by the strings (at most NH; unused slots -> bit 63,
-    // never set in a row index)
-    int hpos[NH];
-    {
-        uint64_t hm = ch.zmask & ~31ull;
-#pragma unroll
-        for (int j = 0; j < NH; ++j)
-        {
-            hpos[j] = hm ? (__ffsll((long long)hm) - 1) : 63;
-            hm &= hm - 1ull;
-        }
-    }
+    // row bits >= 5 used by the strings (at most NH): their marginals live in
+    // shared memory, one (float, float) accumulator per thread each, added to
+    // once per block
+    const uint64_t hmask = ch.zmask & ~31ull;
+    for (int j = 0; j < 2 * NH; ++j)
+        smh[j * 256 + tid] = make_float2(0.f, 0.f);
 
-    T tot[2], totc[2], ml[2][5], mlc[2][5], mh[2][NH], mhc[2][NH];
+    acc tot[2], ml[2][5];
 #pragma unroll
     for (int p = 0; p < 2; ++p)
     {
-        tot[p] = totc[p] = T(0);
+        tot[p] = A::acc_zero();
 #pragma unroll
         for (int j = 0; j < 5; ++j)
-            ml[p][j] = mlc[p][j] = T(0);
-#pragma unroll
-        for (int j = 0; j < NH; ++j)
-            mh[p][j] = mhc[p][j] = T(0);
+            ml[p][j] = A::acc_zero();
     }
 
     if (col_ok)
@@ -187,32 +352,38 @@ __global__ void __launch_bounds__(256, kMargMinBlocks<T>)
             const uint64_t beta = paired ? (((um >> hb) << (hb + 1)) | (um & ((1ull << hb) - 1ull))) : um;
             const uint64_t base = beta << 5;
             const uint64_t baseB = base ^ xh;
-            T bt[2] = {T(0), T(0)};
-            T bl[2][5];
+            val bt[2] = {A::zero(), A::zero()};
+            val bl[2][5];
 #pragma unroll
             for (int p = 0; p < 2; ++p)
 #pragma unroll
                 for (int j = 0; j < 5; ++j)
-                    bl[p][j] = T(0);
+                    bl[p][j] = A::zero();
             if (pl < 0)
-                block_marginals<T, 5>(psi, S, t0, base, baseB, xl, pl, RB, need_re, need_im, bt, bl);
+                block_marginals<A, 5>(psi, S, t0, base, baseB, xl, pl, RB, need_re, need_im, bt, bl, bad);
             else
-                block_marginals<T, 4>(psi, S, t0, base, baseB, xl, pl, RB, need_re, need_im, bt, bl);
+                block_marginals<A, 4>(psi, S, t0, base, baseB, xl, pl, RB, need_re, need_im, bt, bl, bad);
 #pragma unroll
             for (int p = 0; p < 2; ++p)
             {
-                kadd(tot[p], totc[p], bt[p]);
+                A::acc_add(tot[p], bt[p]);
 #pragma unroll
                 for (int j = 0; j < 5; ++j)
-                    kadd(ml[p][j], mlc[p][j], bl[p][j]);
-#pragma unroll
-                for (int j = 0; j < NH; ++j)
-                    if ((base >> hpos[j]) & 1ull)
-                        kadd(mh[p][j], mhc[p][j], bt[p]);
+                    A::acc_add(ml[p][j], bl[p][j]);
+                for (uint64_t w = base & hmask; w; w &= w - 1ull)
+                {
+                    const int b = __ffsll((long long)w) - 1;
+                    float2 *cell = smh + (p * NH + __popcll(hmask & ((1ull << b) - 1ull))) * 256 + tid;
+                    acc a = A::from2(*cell);
+                    A::acc_add(a, bt[p]);
+                    *cell = A::to2(a);
+                }
             }
         }
     }
 
+    if (A::kRaises && bad)
+        atomicOr(range_flag, 1);
     // deterministic float64 reduction over the row lanes, NVB values a pass
 #pragma unroll
     for (int v0 = 0; v0 < NV; v0 += NVB)
@@ -224,14 +395,9 @@ __global__ void __launch_bounds__(256, kMargMinBlocks<T>)
             if (v < NV)
             {
                 const int p = v / (NV / 2), i = v % (NV / 2);
-                double x;
-                if (i == 0)
-                    x = (double)tot[p] - (double)totc[p];
-                else if (i < 6)
-                    x = (double)ml[p][i - 1] - (double)mlc[p][i - 1];
-                else
-                    x = (double)mh[p][i - 6] - (double)mhc[p][i - 6];
-                red[w * 256 + tid] = x;
+                red[w * 256 + tid] = A::to_double(i == 0 ? tot[p]
+                                                         : (i < 6 ? ml[p][i - 1]
+                                                                  : A::from2(smh[(p * NH + i - 6) * 256 + tid])));
             }
         }
         __syncthreads();
@@ -255,7 +421,6 @@ __global__ void __launch_bounds__(256, kMargMinBlocks<T>)
 
     // every string: f * (T - 2 M_b) or f * T; row lanes share the strings
     const uint64_t pbit = paired ? (1ull << (hb + 5)) : (pl >= 0 ? (1ull << pl) : 0ull);
-    const uint64_t hmask = ch.zmask & ~31ull;
     for (int k = tr; k < ch.count; k += TR)
     {
         const int sidx = ch.begin + k;
@@ -279,41 +444,52 @@ __global__ void __launch_bounds__(256, kMargMinBlocks<T>)
     }
 }
 
-template <typename T, int NH>
-void launch_nh(const T *psi, int64_t S, int n, const DevOp &op, const MargChunk *d_chunks, int n_chunks, int TC,
-               int n_ctiles, int n_splits, double *out, cudaStream_t st)
+template <typename A, int NH>
+cudaError_t launch_nh(const void *psi, int64_t S, int n, const DevOp &op, const MargChunk *d_chunks, int n_chunks,
+                      int TC, int n_ctiles, int n_splits, double *out, int *range_flag, cudaStream_t st)
 {
     constexpr int NV = 2 * (1 + 5 + NH);
-    const size_t smem = (size_t)(8 * 256 + NV * TC) * sizeof(double);
+    const size_t smem = (size_t)(8 * 256 + NV * TC) * sizeof(double) + (size_t)2 * NH * 256 * sizeof(float2);
     dim3 grid((unsigned)n_chunks, (unsigned)n_splits, (unsigned)n_ctiles);
-    k_expect_marg<T, NH><<<grid, 256, smem, st>>>(psi, S, n, op.recs, op.orig, op.P, d_chunks, TC, n_splits, out);
+    cudaError_t e = cudaFuncSetAttribute(k_expect_marg<A, NH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    k_expect_marg<A, NH><<<grid, 256, smem, st>>>((const typename A::in_t *)psi, S, n, op.recs, op.orig, op.P,
+                                                  d_chunks, TC, n_splits, out, range_flag);
+    return launched();
+}
+
+template <int NH>
+cudaError_t launch_marg_nh(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const MargChunk *d_chunks,
+                           int n_chunks, int TC, int n_ctiles, int n_splits, double *out, int *range_flag,
+                           const void *psi_df, cudaStream_t st)
+{
+    if (fp32)
+        return launch_nh<ArF32, NH>(psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, nullptr, st);
+    // df64 on the float32 pipes, then the float64 form for out-of-range inputs
+    cudaError_t e =
+        psi_df ? launch_nh<ArDFS, NH>(psi_df, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, nullptr, st)
+               : launch_nh<ArDF, NH>(psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, range_flag, st);
+    if (e != cudaSuccess)
+        return e;
+    return launch_nh<ArF64, NH>(psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, range_flag, st);
 }
 
 } // namespace
 
 cudaError_t launch_expect_marg(bool fp32, const void *psi, int64_t S, int n, const DevOp &op,
                                const MargChunk *d_chunks, int n_chunks, int max_high_bits, int TC, int n_ctiles,
-                               int n_splits, double *out, cudaStream_t st)
+                               int n_splits, double *out, int *range_flag, const void *psi_df, cudaStream_t st)
 {
     if (n_chunks <= 0)
         return cudaSuccess;
     if (max_high_bits > kMargMaxHighBits)
         return cudaErrorInvalidValue;
-#define FPG_MARG(NH)                                                                                                   \
-    if (fp32)                                                                                                          \
-        launch_nh<float, NH>((const float *)psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, st);     \
-    else                                                                                                               \
-        launch_nh<double, NH>((const double *)psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, st);
     if (max_high_bits <= 9)
-    {
-        FPG_MARG(9)
-    }
-    else
-    {
-        FPG_MARG(18)
-    }
-#undef FPG_MARG
-    return launched();
+        return launch_marg_nh<9>(fp32, psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, range_flag,
+                                 psi_df, st);
+    return launch_marg_nh<18>(fp32, psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, range_flag,
+                              psi_df, st);
 }
 
 } // namespace fpg

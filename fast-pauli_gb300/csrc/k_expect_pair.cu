@@ -24,6 +24,7 @@
 // with bit a clear and set are visited side by side when a < 5; for a >= 5
 // bit a is constant over a block.  float32: block sums in float32,
 // Kahan-compensated across blocks, float64 across threads.
+#include "df64.cuh"
 #include "expect_body.cuh"
 
 namespace fpg
@@ -58,14 +59,174 @@ template <typename T> __device__ __forceinline__ void kahan_add(T &acc, T &cmp, 
     }
 }
 
+// complex128 element -> df64 (re_h, re_l, im_h, im_l), integer ops only
+// element e of the state: PRE = the df64 copy (float4 per element, split by
+// k_df_split), else the complex128 state split here
+template <bool PRE> __device__ __forceinline__ void load_df(const void *psi, int64_t e, float (&o)[4], bool &bad)
+{
+    float4 v;
+    if constexpr (PRE)
+        v = __ldg(reinterpret_cast<const float4 *>(psi) + e);
+    else
+        v = split_complex(__ldg(reinterpret_cast<const uint4 *>(psi) + e), bad);
+    o[0] = v.x;
+    o[1] = v.y;
+    o[2] = v.z;
+    o[3] = v.w;
+}
+
+// (re, im) += conj(a) b in df64: re += ar br + ai bi, im += ar bi - ai br
+__device__ __forceinline__ void df_conj_mul_add(const float (&a)[4], const float (&b)[4], float (&re)[2],
+                                                float (&im)[2])
+{
+    df_fma(a[0], a[1], b[0], b[1], re[0], re[1]);
+    df_fma(a[2], a[3], b[2], b[3], re[0], re[1]);
+    df_fma(a[0], a[1], b[2], b[3], im[0], im[1]);
+    df_fma(-a[2], -a[3], b[0], b[1], im[0], im[1]);
+}
+
+// float64 path of the pair kernel on the float32 pipes: the same sums as
+// k_expect_pair<double, 1> with every amplitude split into df64 (df64.cuh);
+// df64 sums per 32-row block, df64 running sums across blocks, float64 only
+// for the final cross-thread reduction.  Error <= ~2^-46 of sum |terms|.
+// An amplitude outside the df64 range raises *range_flag (df64.cuh); with
+// PRE the state comes split already (and checked) by k_df_split.
+template <bool PRE>
+__global__ void __launch_bounds__(256, 2)
+    k_expect_pair_df(const void *__restrict__ psi, int64_t S, int n, const StringRec *__restrict__ recs,
+                     const int32_t *__restrict__ orig, int64_t P, const PairChunk *__restrict__ chunks, int TC,
+                     int n_splits, double *__restrict__ out, int *__restrict__ range_flag)
+{
+    bool bad = false;
+    extern __shared__ double red[]; // blockDim.x doubles
+    const PairChunk ch = chunks[blockIdx.x];
+    const int tid = threadIdx.x;
+    const int tc = tid & (TC - 1);
+    const int tr = tid / TC;
+    const int TR = blockDim.x / TC;
+    const int64_t t0 = (int64_t)blockIdx.z * TC + tc;
+    const bool col_ok = t0 < S;
+
+    const uint64_t D = 1ull << n;
+    const uint64_t xh = ch.x & ~31ull;
+    const uint32_t xl = (uint32_t)ch.x & 31u;
+    const bool paired = xh != 0;
+    const int pl = (!paired && xl != 0u) ? (31 - __clz((int)xl)) : -1;
+    const int64_t NB = n >= 5 ? (int64_t)(D >> 5) : 1;
+    const int RB = n >= 5 ? 32 : (int)D;
+    const int64_t nblk = paired ? NB / 2 : NB;
+    const int hb = paired ? (63 - __clzll((long long)(xh >> 5))) : 0;
+    const int64_t per = (nblk + n_splits - 1) / n_splits;
+    const int64_t b0 = (int64_t)blockIdx.y * per;
+    const int64_t b1 = min(nblk, b0 + per);
+    const int abit = ch.abit;
+    const bool split_in_block = abit >= 0 && abit < 5;
+    const int e1 = split_in_block && pl >= 0 ? min(abit, pl) : (split_in_block ? abit : pl);
+    const int e2 = split_in_block && pl >= 0 ? max(abit, pl) : -1;
+    const int n_rows = 32 >> ((e1 >= 0) + (e2 >= 0));
+
+    // running df64 sums [c][h/l]: U_c^re, U_c^im
+    float ure[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, uim[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    if (col_ok)
+    {
+        for (int64_t m = b0 + tr; m < b1; m += TR)
+        {
+            const uint64_t um = (uint64_t)m;
+            const uint64_t beta = paired ? (((um >> hb) << (hb + 1)) | (um & ((1ull << hb) - 1ull))) : um;
+            const uint64_t base = beta << 5;
+            const uint64_t baseB = base ^ xh;
+            float sre[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, sim[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll 2
+            for (int m2 = 0; m2 < n_rows; ++m2)
+            {
+                uint32_t r0 = (uint32_t)m2;
+                if (e1 >= 0)
+                    r0 = ((r0 >> e1) << (e1 + 1)) | (r0 & ((1u << e1) - 1u));
+                if (e2 >= 0)
+                    r0 = ((r0 >> e2) << (e2 + 1)) | (r0 & ((1u << e2) - 1u));
+                if ((int)r0 < RB)
+                {
+                    float a[4], b[4];
+                    load_df<PRE>(psi, (int64_t)(base + r0) * S + t0, a, bad);
+                    load_df<PRE>(psi, (int64_t)(baseB + (r0 ^ xl)) * S + t0, b, bad);
+                    if (split_in_block)
+                    {
+                        const uint32_t r1 = r0 | (1u << abit);
+                        float c[4], d[4];
+                        load_df<PRE>(psi, (int64_t)(base + r1) * S + t0, c, bad);
+                        load_df<PRE>(psi, (int64_t)(baseB + (r1 ^ xl)) * S + t0, d, bad);
+                        df_conj_mul_add(c, d, sre[1], sim[1]);
+                    }
+                    df_conj_mul_add(a, b, sre[0], sim[0]);
+                }
+            }
+            const int c0 = (abit >= 5) ? (int)((base >> abit) & 1u) : 0;
+            if (c0 == 0)
+            {
+                df_add(ure[0][0], ure[0][1], sre[0][0], sre[0][1]);
+                df_add(uim[0][0], uim[0][1], sim[0][0], sim[0][1]);
+            }
+            else
+            {
+                df_add(ure[1][0], ure[1][1], sre[0][0], sre[0][1]);
+                df_add(uim[1][0], uim[1][1], sim[0][0], sim[0][1]);
+            }
+            if (split_in_block)
+            {
+                df_add(ure[1][0], ure[1][1], sre[1][0], sre[1][1]);
+                df_add(uim[1][0], uim[1][1], sim[1][0], sim[1][1]);
+            }
+        }
+    }
+
+    if (!PRE && bad)
+        atomicOr(range_flag, 1);
+    // float64 reduction of the four sums over the row lanes (fixed order)
+    double tot[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+    {
+        const float *u = q == 0 ? ure[0] : q == 1 ? ure[1] : q == 2 ? uim[0] : uim[1];
+        red[tr * TC + tc] = df_to_double(u[0], u[1]);
+        __syncthreads();
+        for (int s = TR >> 1; s > 0; s >>= 1)
+        {
+            if (tr < s)
+                red[tr * TC + tc] += red[(tr + s) * TC + tc];
+            __syncthreads();
+        }
+        tot[q] = red[tc];
+        __syncthreads();
+    }
+    if (tr != 0 || !col_ok)
+        return;
+    const uint64_t pbit = paired ? (1ull << (hb + 5)) : (pl >= 0 ? (1ull << pl) : 0ull);
+    for (int k = 0; k < ch.count; ++k)
+    {
+        const int sidx = ch.begin + k;
+        const StringRec rec = recs[sidx];
+        const bool odd = (rec.meta & 1u) != 0;
+        const bool flip = ((rec.z & ~pbit) != 0);
+        const int ny = (int)(rec.meta & 3u);
+        const double f = ((ny & 2) ? -1.0 : 1.0) * (pbit ? 2.0 : 1.0);
+        const double u0 = odd ? tot[2] : tot[0];
+        const double u1 = odd ? tot[3] : tot[1];
+        out[((int64_t)blockIdx.y * P + orig[sidx]) * S + t0] = f * (flip ? u0 - u1 : u0 + u1);
+    }
+}
+
 template <typename T, int V> constexpr int kPairMinBlocks = sizeof(T) == 4 ? 3 : 1;
 
+// only_if: when not null, the launch is the float64 recomputation after the
+// df64 kernel and returns at once unless *only_if is set.
 template <typename T, int V>
 __global__ void __launch_bounds__(256, kPairMinBlocks<T, V>)
     k_expect_pair(const T *__restrict__ psi, int64_t S, int n, const StringRec *__restrict__ recs,
                   const int32_t *__restrict__ orig, int64_t P, const PairChunk *__restrict__ chunks, int TC,
-                  int n_splits, double *__restrict__ out)
+                  int n_splits, double *__restrict__ out, const int *__restrict__ only_if)
 {
+    if (only_if && *only_if == 0)
+        return;
     extern __shared__ double red[]; // blockDim.x * V doubles
     const PairChunk ch = chunks[blockIdx.x];
     const int tid = threadIdx.x;
@@ -220,21 +381,33 @@ __global__ void __launch_bounds__(256, kPairMinBlocks<T, V>)
 } // namespace
 
 cudaError_t launch_expect_pair(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const PairChunk *d_chunks,
-                               int n_chunks, const ExpectPlan &plan, double *out, cudaStream_t st)
+                               int n_chunks, const ExpectPlan &plan, double *out, int *range_flag,
+                               const void *psi_df, cudaStream_t st)
 {
     if (n_chunks <= 0)
         return cudaSuccess;
     dim3 grid((unsigned)n_chunks, (unsigned)plan.n_splits, (unsigned)plan.n_ctiles);
     const size_t smem = 256 * plan.V * sizeof(double);
     if (!fp32)
+    {
+        // df64 on the float32 pipes, then the float64 form for out-of-range inputs
+        if (psi_df)
+            k_expect_pair_df<true><<<grid, 256, smem, st>>>(psi_df, S, n, op.recs, op.orig, op.P, d_chunks, plan.TC,
+                                                            plan.n_splits, out, range_flag);
+        else
+            k_expect_pair_df<false><<<grid, 256, smem, st>>>(psi, S, n, op.recs, op.orig, op.P, d_chunks, plan.TC,
+                                                             plan.n_splits, out, range_flag);
+        if (cudaError_t e = launched())
+            return e;
         k_expect_pair<double, 1><<<grid, 256, smem, st>>>((const double *)psi, S, n, op.recs, op.orig, op.P, d_chunks,
-                                                          plan.TC, plan.n_splits, out);
+                                                          plan.TC, plan.n_splits, out, range_flag);
+    }
     else if (plan.V == 2)
         k_expect_pair<float, 2><<<grid, 256, smem, st>>>((const float *)psi, S, n, op.recs, op.orig, op.P, d_chunks,
-                                                         plan.TC, plan.n_splits, out);
+                                                         plan.TC, plan.n_splits, out, nullptr);
     else
         k_expect_pair<float, 1><<<grid, 256, smem, st>>>((const float *)psi, S, n, op.recs, op.orig, op.P, d_chunks,
-                                                         plan.TC, plan.n_splits, out);
+                                                         plan.TC, plan.n_splits, out, nullptr);
     return launched();
 }
 

@@ -12,8 +12,7 @@
 // 16 rows, instead of one add per row.  For a group of G strings the cost per
 // row drops from ~4 + G to ~4 + 4 + G/16 operations (q, transform, lookups),
 // which is what makes large groups (e.g. the 105 Z-type strings of a
-// weight <= 2 set, or the 28 strings sharing one X/Y position) cheap on
-// GB300's narrow float64 pipe.
+// weight <= 2 set) cheap.
 //
 // CTA: 128 threads = TC column lanes x TR row lanes.  A round: every row lane
 // transforms one 16-row block (both parts, Re and Im, when the chunk has
@@ -21,50 +20,216 @@
 // thread sums, for its own strings (string k belongs to row lane k % TR), the
 // TR blocks of the round with the block-parity sign.  Each (string, column)
 // accumulator lives in exactly one thread: no cross-thread reduction.
-// float32 path: one Kahan-compensated add per string per round.
+//
+// Arithmetic (the policy W): complex64 states in float32 with one
+// Kahan-compensated add per string per round; complex128 states in
+// double-float (df64.cuh) on the float32 pipes, the state split once per call
+// (k_df_split), followed by the float64 form, which recomputes only when the
+// call's range flag was raised.
 #include "common.cuh"
+#include "df64.cuh"
 
 namespace fpg
 {
 namespace
 {
 
-template <typename T> struct C2t;
-template <> struct C2t<double>
+struct DFv
 {
-    using type = double2;
-};
-template <> struct C2t<float>
-{
-    using type = float2;
+    float h, l;
 };
 
-template <typename T> __device__ __forceinline__ void wht16(T (&v)[16])
+// complex64 states
+struct W32
+{
+    using in_t = float2;
+    using val = float;
+    using cell = float; // shared-memory type of a transform value
+    struct acc
+    {
+        float v, c;
+    };
+    static constexpr bool kRecompute = false;
+    static __device__ __forceinline__ val zero()
+    {
+        return 0.f;
+    }
+    static __device__ __forceinline__ void q(const in_t *psi, int64_t ea, int64_t eb, bool re, bool im, val &vr,
+                                             val &vi)
+    {
+        const float2 a = __ldg(psi + ea), b = __ldg(psi + eb);
+        if (re)
+            vr = fmaf(a.x, b.x, a.y * b.y);
+        if (im)
+            vi = fmaf(a.x, b.y, -(a.y * b.x));
+    }
+    static __device__ __forceinline__ void butterfly(val &a, val &b)
+    {
+        const val s = a + b, d = a - b;
+        a = s;
+        b = d;
+    }
+    static __device__ __forceinline__ cell to_cell(val v)
+    {
+        return v;
+    }
+    static __device__ __forceinline__ void add_cell(val &s, cell c, bool neg)
+    {
+        s += neg ? -c : c;
+    }
+    static __device__ __forceinline__ acc acc_zero()
+    {
+        return acc{0.f, 0.f};
+    }
+    static __device__ __forceinline__ void acc_add(acc &a, val x)
+    {
+        const float y = x - a.c;
+        const float s = a.v + y;
+        a.c = (s - a.v) - y;
+        a.v = s;
+    }
+    static __device__ __forceinline__ double to_double(const acc &a)
+    {
+        return (double)a.v - (double)a.c;
+    }
+};
+
+// complex128 states, float64 arithmetic (the recomputation)
+struct W64
+{
+    using in_t = double2;
+    using val = double;
+    using cell = double;
+    using acc = double;
+    static constexpr bool kRecompute = true;
+    static __device__ __forceinline__ val zero()
+    {
+        return 0.0;
+    }
+    static __device__ __forceinline__ void q(const in_t *psi, int64_t ea, int64_t eb, bool re, bool im, val &vr,
+                                             val &vi)
+    {
+        const double2 a = __ldg(psi + ea), b = __ldg(psi + eb);
+        if (re)
+            vr = fma(a.x, b.x, a.y * b.y);
+        if (im)
+            vi = fma(a.x, b.y, -(a.y * b.x));
+    }
+    static __device__ __forceinline__ void butterfly(val &a, val &b)
+    {
+        const val s = a + b, d = a - b;
+        a = s;
+        b = d;
+    }
+    static __device__ __forceinline__ cell to_cell(val v)
+    {
+        return v;
+    }
+    static __device__ __forceinline__ void add_cell(val &s, cell c, bool neg)
+    {
+        s += neg ? -c : c;
+    }
+    static __device__ __forceinline__ acc acc_zero()
+    {
+        return 0.0;
+    }
+    static __device__ __forceinline__ void acc_add(acc &a, val x)
+    {
+        a += x;
+    }
+    static __device__ __forceinline__ double to_double(const acc &a)
+    {
+        return a;
+    }
+};
+
+// complex128 states split into df64 (float4 per element): df64 arithmetic
+struct WDF
+{
+    using in_t = float4;
+    using val = DFv;
+    using cell = float2;
+    using acc = DFv;
+    static constexpr bool kRecompute = false;
+    static __device__ __forceinline__ val zero()
+    {
+        return DFv{0.f, 0.f};
+    }
+    static __device__ __forceinline__ void q(const in_t *psi, int64_t ea, int64_t eb, bool re, bool im, val &vr,
+                                             val &vi)
+    {
+        const float4 a = __ldg(psi + ea), b = __ldg(psi + eb);
+        if (re)
+        {
+            vr = DFv{0.f, 0.f};
+            df_fma(a.x, a.y, b.x, b.y, vr.h, vr.l);
+            df_fma(a.z, a.w, b.z, b.w, vr.h, vr.l);
+        }
+        if (im)
+        {
+            vi = DFv{0.f, 0.f};
+            df_fma(a.x, a.y, b.z, b.w, vi.h, vi.l);
+            df_fma(-a.z, -a.w, b.x, b.y, vi.h, vi.l);
+        }
+    }
+    static __device__ __forceinline__ void butterfly(val &a, val &b)
+    {
+        DFv s = a, d = a;
+        df_add(s.h, s.l, b.h, b.l);
+        df_add(d.h, d.l, -b.h, -b.l);
+        a = s;
+        b = d;
+    }
+    static __device__ __forceinline__ cell to_cell(val v)
+    {
+        return make_float2(v.h, v.l);
+    }
+    static __device__ __forceinline__ void add_cell(val &s, cell c, bool neg)
+    {
+        df_add(s.h, s.l, neg ? -c.x : c.x, neg ? -c.y : c.y);
+    }
+    static __device__ __forceinline__ acc acc_zero()
+    {
+        return DFv{0.f, 0.f};
+    }
+    static __device__ __forceinline__ void acc_add(acc &a, val x)
+    {
+        df_add(a.h, a.l, x.h, x.l);
+    }
+    static __device__ __forceinline__ double to_double(const acc &a)
+    {
+        return df_to_double(a.h, a.l);
+    }
+};
+
+template <typename W> __device__ __forceinline__ void wht16(typename W::val (&v)[16])
 {
 #pragma unroll
     for (int s = 1; s < 16; s <<= 1)
 #pragma unroll
         for (int r = 0; r < 16; ++r)
             if (!(r & s))
-            {
-                const T a = v[r], b = v[r | s];
-                v[r] = a + b;
-                v[r | s] = a - b;
-            }
+                W::butterfly(v[r], v[r | s]);
 }
 
-template <typename T, int SLOTS>
+// only_if: when not null, the float64 recomputation returns at once unless
+// *only_if is set.
+template <typename W, int SLOTS>
 __global__ void __launch_bounds__(128)
-    k_expect_wht(const T *__restrict__ psi, int64_t S, int n, const StringRec *__restrict__ recs,
+    k_expect_wht(const typename W::in_t *__restrict__ psi, int64_t S, int n, const StringRec *__restrict__ recs,
                  const int32_t *__restrict__ orig, int64_t P, const WhtChunk *__restrict__ chunks, int TC,
-                 int n_splits, double *__restrict__ out)
+                 int n_splits, double *__restrict__ out, const int *__restrict__ only_if)
 {
-    using CT = typename C2t<T>::type;
+    using val = typename W::val;
+    using cell = typename W::cell;
+    using acc = typename W::acc;
+    if (W::kRecompute && only_if && *only_if == 0)
+        return;
     extern __shared__ unsigned char smem_raw[];
     const int TR = blockDim.x / TC;
-    T *wsm = reinterpret_cast<T *>(smem_raw);                  // [2][TR][16][TC]
-    uint64_t *s_base = reinterpret_cast<uint64_t *>(wsm + 2 * TR * 16 * TC); // [TR], ~0 = no block
-    uint64_t *s_z = s_base + TR;                                             // [count] z masks of the chunk
+    cell *wsm = reinterpret_cast<cell *>(smem_raw);                                // [2][TR][16][TC]
+    uint64_t *s_base = reinterpret_cast<uint64_t *>(smem_raw + (size_t)2 * TR * 16 * TC * 8); // [TR], ~0 = no block
+    uint64_t *s_z = s_base + TR;                                                   // [count] z masks of the chunk
 
     const WhtChunk ch = chunks[blockIdx.x];
     const int tid = threadIdx.x;
@@ -89,25 +254,21 @@ __global__ void __launch_bounds__(128)
     // chunk strings' z masks in shared memory; this thread owns k = tr + j * TR
     for (int k = tid; k < G; k += blockDim.x)
         s_z[k] = recs[ch.begin + k].z;
-    T acc[SLOTS];
-    T cmp[sizeof(T) == 4 ? SLOTS : 1]; // Kahan compensation (float32 only)
+    acc sums[SLOTS];
 #pragma unroll
     for (int j = 0; j < SLOTS; ++j)
-        acc[j] = T(0);
-#pragma unroll
-    for (int j = 0; j < (int)(sizeof(cmp) / sizeof(T)); ++j)
-        cmp[j] = T(0);
+        sums[j] = W::acc_zero();
     __syncthreads();
 
     for (int64_t mr = b0; mr < b1; mr += TR)
     {
         const int64_t m = mr + tr;
-        T vre[16], vim[16];
+        val vre[16], vim[16];
 #pragma unroll
         for (int r = 0; r < 16; ++r)
         {
-            vre[r] = T(0);
-            vim[r] = T(0);
+            vre[r] = W::zero();
+            vim[r] = W::zero();
         }
         uint64_t base = ~0ull;
         if (m < b1)
@@ -118,33 +279,26 @@ __global__ void __launch_bounds__(128)
             if (col_ok)
             {
                 const uint64_t baseB = base ^ xh;
-                const CT *ps = reinterpret_cast<const CT *>(psi);
 #pragma unroll
                 for (int r = 0; r < 16; ++r)
                     if (r < RB)
-                    {
-                        const CT a = __ldg(ps + (int64_t)(base + r) * S + t0);
-                        const CT b = __ldg(ps + (int64_t)(baseB + (uint64_t)(r ^ xl)) * S + t0);
-                        if (need_re)
-                            vre[r] = fma(a.x, b.x, a.y * b.y);
-                        if (need_im)
-                            vim[r] = fma(a.x, b.y, -(a.y * b.x));
-                    }
+                        W::q(psi, (int64_t)(base + r) * S + t0, (int64_t)(baseB + (uint64_t)(r ^ xl)) * S + t0, need_re,
+                             need_im, vre[r], vim[r]);
             }
         }
         if (need_re)
-            wht16(vre);
+            wht16<W>(vre);
         if (need_im)
-            wht16(vim);
-        T *w0 = wsm + (size_t)(tr * 16) * TC + tc;             // part 0 (Re)
-        T *w1 = wsm + (size_t)((TR + tr) * 16) * TC + tc;      // part 1 (Im)
+            wht16<W>(vim);
+        cell *w0 = wsm + (size_t)(tr * 16) * TC + tc;        // part 0 (Re)
+        cell *w1 = wsm + (size_t)((TR + tr) * 16) * TC + tc; // part 1 (Im)
 #pragma unroll
         for (int u = 0; u < 16; ++u)
         {
             if (need_re)
-                w0[u * TC] = vre[u];
+                w0[u * TC] = W::to_cell(vre[u]);
             if (need_im)
-                w1[u * TC] = vim[u];
+                w1[u * TC] = W::to_cell(vim[u]);
         }
         if (tc == 0)
             s_base[tr] = base;
@@ -158,24 +312,11 @@ __global__ void __launch_bounds__(128)
                 break;
             const uint64_t z = s_z[k];
             const int part = k >= ch.n_even ? 1 : 0; // odd #Y strings read the Im transform
-            const T *wp = wsm + (size_t)((part * TR * 16) + (int)(z & 15u)) * TC + tc;
-            T sum = T(0);
+            const cell *wp = wsm + (size_t)((part * TR * 16) + (int)(z & 15u)) * TC + tc;
+            val sum = W::zero();
             for (int rr = 0; rr < nb; ++rr)
-            {
-                const T w = wp[(size_t)rr * 16 * TC];
-                sum += (__popcll(s_base[rr] & z) & 1) ? -w : w;
-            }
-            if constexpr (sizeof(T) == 8)
-            {
-                acc[j] += sum;
-            }
-            else
-            {
-                const T y = sum - cmp[j];
-                const T s = acc[j] + y;
-                cmp[j] = (s - acc[j]) - y;
-                acc[j] = s;
-            }
+                W::add_cell(sum, wp[(size_t)rr * 16 * TC], (__popcll(s_base[rr] & z) & 1) != 0);
+            W::acc_add(sums[j], sum);
         }
         __syncthreads();
     }
@@ -191,45 +332,58 @@ __global__ void __launch_bounds__(128)
         const int sidx = ch.begin + k;
         const int ny = (int)(recs[sidx].meta & 3u);
         const double f = ((ny & 2) ? -1.0 : 1.0) * (paired ? 2.0 : 1.0);
-        double v = (double)acc[j];
-        if constexpr (sizeof(T) == 4)
-            v -= (double)cmp[j];
-        out[((int64_t)blockIdx.y * P + orig[sidx]) * S + t0] = f * v;
+        out[((int64_t)blockIdx.y * P + orig[sidx]) * S + t0] = f * W::to_double(sums[j]);
     }
+}
+
+template <typename W, int SL>
+cudaError_t launch_w(const void *psi, int64_t S, int n, const DevOp &op, const WhtChunk *d_chunks, int n_chunks,
+                     int TC, int n_ctiles, int n_splits, double *out, const int *only_if, size_t smem, cudaStream_t st)
+{
+    dim3 grid((unsigned)n_chunks, (unsigned)n_splits, (unsigned)n_ctiles);
+    k_expect_wht<W, SL><<<grid, 128, smem, st>>>((const typename W::in_t *)psi, S, n, op.recs, op.orig, op.P,
+                                                 d_chunks, TC, n_splits, out, only_if);
+    return launched();
+}
+
+template <int SL>
+cudaError_t launch_sl(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const WhtChunk *d_chunks,
+                      int n_chunks, int TC, int n_ctiles, int n_splits, double *out, int *range_flag,
+                      const void *psi_df, size_t smem, cudaStream_t st)
+{
+    if (fp32)
+        return launch_w<W32, SL>(psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, nullptr, smem, st);
+    if (psi_df)
+    {
+        if (cudaError_t e = launch_w<WDF, SL>(psi_df, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out,
+                                              nullptr, smem, st))
+            return e;
+        return launch_w<W64, SL>(psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, range_flag, smem,
+                                 st);
+    }
+    // no df64 copy of the state: float64 throughout
+    return launch_w<W64, SL>(psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, nullptr, smem, st);
 }
 
 } // namespace
 
 cudaError_t launch_expect_wht(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const WhtChunk *d_chunks,
                               int n_chunks, int max_count, int TC, int n_ctiles, int n_splits, double *out,
-                              cudaStream_t st)
+                              int *range_flag, const void *psi_df, cudaStream_t st)
 {
     if (n_chunks <= 0)
         return cudaSuccess;
     const int threads = 128;
     const int TR = threads / TC;
     const int slots_needed = (max_count + TR - 1) / TR;
-    const size_t smem = (size_t)2 * TR * 16 * TC * (fp32 ? 4 : 8) + (size_t)TR * 8 + (size_t)max_count * 8;
-    dim3 grid((unsigned)n_chunks, (unsigned)n_splits, (unsigned)n_ctiles);
-#define FPG_WHT(SL)                                                                                                    \
-    if (fp32)                                                                                                          \
-        k_expect_wht<float, SL><<<grid, threads, smem, st>>>((const float *)psi, S, n, op.recs, op.orig, op.P,        \
-                                                             d_chunks, TC, n_splits, out);                            \
-    else                                                                                                               \
-        k_expect_wht<double, SL><<<grid, threads, smem, st>>>((const double *)psi, S, n, op.recs, op.orig, op.P,      \
-                                                              d_chunks, TC, n_splits, out);
+    const size_t smem = (size_t)2 * TR * 16 * TC * 8 + (size_t)TR * 8 + (size_t)max_count * 8;
     if (slots_needed <= 8)
-    {
-        FPG_WHT(8)
-    }
-    else if (slots_needed <= 32)
-    {
-        FPG_WHT(32)
-    }
-    else
-        return cudaErrorInvalidValue;
-#undef FPG_WHT
-    return launched();
+        return launch_sl<8>(fp32, psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, range_flag, psi_df,
+                            smem, st);
+    if (slots_needed <= 32)
+        return launch_sl<32>(fp32, psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, range_flag, psi_df,
+                             smem, st);
+    return cudaErrorInvalidValue;
 }
 
 } // namespace fpg

@@ -13,6 +13,10 @@
 //    admits every request that fits (smaller ones may pass a large one that
 //    does not fit yet).  A request larger than the whole budget is refused at
 //    submission (FPG_ERR_BUSY).
+//  * Priorities: half of the slots are streams of the device's highest
+//    priority, reserved for small requests (<= kSmallWork amplitude-terms);
+//    the block scheduler starts their CTAs ahead of the large requests' as
+//    SMs free up, so short requests are not stuck behind long ones.
 //  * Continuous: the scheduler thread admits new requests the moment slots
 //    and memory free up, while earlier requests are still running; admitted
 //    requests run concurrently on their slots' streams, so their kernels
@@ -23,6 +27,7 @@
 //  * Latency per ticket: submit -> admission -> completion (host steady
 //    clock, completion observed through a CUDA event).
 #include <algorithm>
+#include <cmath>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -57,7 +62,13 @@ struct Ticket
     std::string err;
     clock_type::time_point t_submit, t_start, t_done;
     int slot = -1;
+    bool small = false; // work <= kSmallWork amplitude-terms
 };
+
+// Requests of at most this many amplitude-terms (n_strings * 2^n * n_states,
+// a few milliseconds of GPU time) count as small and run on high-priority
+// slots.
+constexpr double kSmallWork = 4.0e9;
 
 } // namespace
 
@@ -76,6 +87,7 @@ struct fpg_server
         cudaEvent_t event = nullptr;
         uint64_t ticket = 0;
         bool busy = false;
+        bool high = false; // created with the device's highest stream priority
     };
     std::vector<Slot> slots;
     size_t reserved = 0;
@@ -161,10 +173,20 @@ void fpg_server::run()
         // 2. admit queued requests into free slots while the budget allows
         for (auto it = queue.begin(); it != queue.end();)
         {
-            auto free_slot = std::find_if(slots.begin(), slots.end(), [](const Slot &s) { return !s.busy; });
-            if (free_slot == slots.end())
-                break;
             Ticket &t = tickets[*it];
+            // small requests take a high-priority slot when one is free (else any
+            // free slot); large ones only normal slots, so that small requests
+            // always find a stream whose work the GPU schedules first
+            auto free_slot = slots.end();
+            if (t.small)
+                free_slot = std::find_if(slots.begin(), slots.end(), [](const Slot &s) { return !s.busy && s.high; });
+            if (free_slot == slots.end())
+                free_slot = std::find_if(slots.begin(), slots.end(), [](const Slot &s) { return !s.busy && !s.high; });
+            if (free_slot == slots.end())
+            {
+                ++it; // no slot of its class: later requests of the other class may pass
+                continue;
+            }
             if (reserved + t.need > (size_t)cfg.hbm_budget_bytes)
             {
                 ++it; // does not fit yet: let later, smaller requests pass
@@ -231,10 +253,18 @@ extern "C"
             s->cfg.max_queue = 1 << 20;
         cudaError_t e = cudaGetDevice(&s->device);
         s->slots.resize((size_t)config->n_slots);
-        for (auto &sl : s->slots)
+        // the first half of the slots (none when there is one) run at the
+        // highest stream priority and serve small requests
+        int prio_low = 0, prio_high = 0;
+        if (e == cudaSuccess)
+            e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+        const int n_high = config->n_slots > 1 ? config->n_slots / 2 : 0;
+        for (size_t i = 0; i < s->slots.size(); ++i)
         {
+            auto &sl = s->slots[i];
+            sl.high = (int)i < n_high;
             if (e == cudaSuccess)
-                e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+                e = cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking, sl.high ? prio_high : prio_low);
             if (e == cudaSuccess)
                 e = cudaEventCreateWithFlags(&sl.event, cudaEventDisableTiming);
         }
@@ -286,6 +316,12 @@ extern "C"
         Ticket t;
         t.req = *req;
         t.need = need;
+        {
+            int32_t nq = 0;
+            int64_t ps = 0;
+            fpg_operator_info(req->op, &nq, &ps, nullptr);
+            t.small = (double)ps * std::ldexp(1.0, nq) * (double)req->n_states <= kSmallWork;
+        }
         t.t_submit = clock_type::now();
         s->tickets.emplace(id, std::move(t));
         s->queue.push_back(id);

@@ -200,6 +200,26 @@ def test_marginal_kernel_groups_per_string(n, S):
     op.close()
 
 
+@pytest.mark.parametrize("scale_psi,scale_h", [(1.0, 1.0), (1e-30, 1.0), (1e15, 1.0), (1.0, 1e20), (1.0, 1e-35)])
+def test_float64_path_far_from_unit_scale(scale_psi, scale_h):
+    """The float64 path runs its kernels in double-float arithmetic on the
+    float32 pipes for values within 2^-90 .. 2^40 and recomputes in float64
+    otherwise: results must meet the float64 tolerance at any scale, and for
+    states with exact zeros (basis states)."""
+    rng = np.random.default_rng(61)
+    n, S, K = 9, 12, 5
+    strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
+    P = len(strings)
+    h = (rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))) * scale_h
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    psi[:, 0] = 0
+    psi[5, 0] = 1.0  # a basis state: all other amplitudes exactly zero
+    psi *= scale_psi
+    want = oracle.summed_expectation(strings, h, psi)
+    got = fp.SummedPauliOp(strings, h).expectation_value(psi)
+    assert normwise(got, want) < TOL_C128
+
+
 def test_exhaustive_small_strings_vs_dense():
     rng = np.random.default_rng(3)
     for n in (1, 2, 3):
