@@ -220,6 +220,7 @@ void build_fast_decomposition(fpg_operator *op)
 {
     op->wht.clear();
     op->wht_max_count = 0;
+    op->wht_both = false;
     op->pairs.clear();
     op->margs.clear();
     op->marg_max_high = 0;
@@ -268,6 +269,7 @@ void build_fast_decomposition(fpg_operator *op)
             const int32_t ne = std::max<int32_t>(0, std::min<int32_t>(cnt, n_even_total - b));
             op->wht.push_back(WhtChunk{g.x, g.begin + b, (int16_t)cnt, (int16_t)ne});
             op->wht_max_count = std::max(op->wht_max_count, (int)cnt);
+            op->wht_both = op->wht_both || (ne > 0 && ne < cnt);
         }
     }
     // direct chunks of the remaining groups, in the order of the full decomposition
@@ -392,7 +394,7 @@ ExpectPlan plan_expect(const fpg_operator *op, int64_t S, bool fp32, const void 
     p.fam_splits[kFamMarg] =
         pick((int64_t)op->margs.size() * p.wht_ctiles, NB / 2, 256 / p.wht_TC, over1, kWindowBlocks);
     p.fam_splits[kFamWht] =
-        pick((int64_t)op->wht.size() * p.wht_ctiles, NB16 / 2, 128 / p.wht_TC, over1, 2 * kWindowBlocks);
+        pick((int64_t)op->wht.size() * p.wht_ctiles, NB16 / 2, kWhtThreads / p.wht_TC, over1, 2 * kWindowBlocks);
     p.n_splits = 1;
     for (int f = 0; f < kNumFam; ++f)
         p.n_splits = std::max(p.n_splits, p.fam_splits[f]);
@@ -462,7 +464,7 @@ int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int6
     {
         double *dst = target(kFamWht, d, pl);
         FPG_CUDA(launch_expect_wht(fp32, psi, S, op->n, d, op->d_wht, (int)op->wht.size(), op->wht_max_count,
-                                   pl.wht_TC, pl.wht_ctiles, pl.n_splits, dst, range_flag, psi_df, st));
+                                   op->wht_both, pl.wht_TC, pl.wht_ctiles, pl.n_splits, dst, range_flag, psi_df, st));
     }
     if (!op->margs.empty())
     {

@@ -63,6 +63,7 @@ struct WhtChunk
 };
 constexpr int kWhtMinStrings = 10;
 constexpr int kWhtMaxStrings = 128;
+constexpr int kWhtThreads = 256; // CTA of the transform kernel
 
 // Work unit of the pair kernel (k_expect_pair.cu): a whole x-group of at most
 // kPairMaxStrings strings [begin, begin + count) whose signs, after dropping
@@ -206,13 +207,15 @@ cudaError_t launch_df_split(const void *psi, int64_t count, void *out, int *rang
 // copy once per call instead of inside every kernel.
 constexpr int64_t kDfSplitMaxBytes = int64_t(16) << 30;
 
-// Transform kernel over WHT chunks (128 threads = TC column lanes x 128/TC row
-// lanes, one complex element per lane); writes like launch_expect_chunks.
+// Transform kernel over WHT chunks (kWhtThreads = TC column lanes x
+// kWhtThreads/TC row lanes, one complex element per lane); writes like
+// launch_expect_chunks.
 // complex128: df64 on psi_df then the float64 recomputation gated by
 // *range_flag, or float64 alone when psi_df is null.
+// both_parts: some chunk has strings of both #Y parities.
 cudaError_t launch_expect_wht(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const WhtChunk *d_chunks,
-                              int n_chunks, int max_count, int TC, int n_ctiles, int n_splits, double *out,
-                              int *range_flag, const void *psi_df, cudaStream_t st);
+                              int n_chunks, int max_count, bool both_parts, int TC, int n_ctiles, int n_splits,
+                              double *out, int *range_flag, const void *psi_df, cudaStream_t st);
 
 // out(K,S) += H^T(K,P) * E(P,S); H complex (P,K), E real float64 (P,S).
 // out complex128 (fp32=false) or complex64 (fp32=true).

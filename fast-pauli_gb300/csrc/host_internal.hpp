@@ -49,6 +49,7 @@ struct fpg_operator
     std::vector<int> fast_class_begin;
     std::vector<fpg::WhtChunk> wht;
     int wht_max_count = 0;
+    bool wht_both = false; // some transform chunk has strings of both #Y parities
     std::vector<fpg::PairChunk> pairs; // groups served by the pair kernel
     fpg::PairChunk *d_pairs = nullptr;
     std::vector<fpg::MargChunk> margs; // groups served by the marginal kernel

@@ -136,29 +136,52 @@ __global__ void __launch_bounds__(256, 2)
             const uint64_t base = beta << 5;
             const uint64_t baseB = base ^ xh;
             float sre[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, sim[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
-#pragma unroll 2
-            for (int m2 = 0; m2 < n_rows; ++m2)
+            // four visited rows at a time, all their loads issued before any use
+            // (the kernel is bound by L2 latency); n_rows is 8, 16 or 32
+            for (int m0 = 0; m0 < n_rows; m0 += 4)
             {
-                uint32_t r0 = (uint32_t)m2;
-                if (e1 >= 0)
-                    r0 = ((r0 >> e1) << (e1 + 1)) | (r0 & ((1u << e1) - 1u));
-                if (e2 >= 0)
-                    r0 = ((r0 >> e2) << (e2 + 1)) | (r0 & ((1u << e2) - 1u));
-                if ((int)r0 < RB)
+                uint32_t r0[4];
+                bool ok[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
                 {
-                    float a[4], b[4];
-                    load_df<PRE>(psi, (int64_t)(base + r0) * S + t0, a, bad);
-                    load_df<PRE>(psi, (int64_t)(baseB + (r0 ^ xl)) * S + t0, b, bad);
-                    if (split_in_block)
-                    {
-                        const uint32_t r1 = r0 | (1u << abit);
-                        float c[4], d[4];
-                        load_df<PRE>(psi, (int64_t)(base + r1) * S + t0, c, bad);
-                        load_df<PRE>(psi, (int64_t)(baseB + (r1 ^ xl)) * S + t0, d, bad);
-                        df_conj_mul_add(c, d, sre[1], sim[1]);
-                    }
-                    df_conj_mul_add(a, b, sre[0], sim[0]);
+                    uint32_t r = (uint32_t)(m0 + u);
+                    if (e1 >= 0)
+                        r = ((r >> e1) << (e1 + 1)) | (r & ((1u << e1) - 1u));
+                    if (e2 >= 0)
+                        r = ((r >> e2) << (e2 + 1)) | (r & ((1u << e2) - 1u));
+                    r0[u] = r;
+                    ok[u] = (int)r < RB;
                 }
+                float a[4][4], b[4][4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (ok[u])
+                    {
+                        load_df<PRE>(psi, (int64_t)(base + r0[u]) * S + t0, a[u], bad);
+                        load_df<PRE>(psi, (int64_t)(baseB + (r0[u] ^ xl)) * S + t0, b[u], bad);
+                    }
+                if (split_in_block)
+                {
+                    // rows r1 = r0 | 2^a (< RB as a < n)
+                    float c[4][4], d[4][4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (ok[u])
+                        {
+                            const uint32_t r1 = r0[u] | (1u << abit);
+                            load_df<PRE>(psi, (int64_t)(base + r1) * S + t0, c[u], bad);
+                            load_df<PRE>(psi, (int64_t)(baseB + (r1 ^ xl)) * S + t0, d[u], bad);
+                        }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (ok[u])
+                            df_conj_mul_add(c[u], d[u], sre[1], sim[1]);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (ok[u])
+                        df_conj_mul_add(a[u], b[u], sre[0], sim[0]);
             }
             const int c0 = (abit >= 5) ? (int)((base >> abit) & 1u) : 0;
             if (c0 == 0)
@@ -215,7 +238,9 @@ __global__ void __launch_bounds__(256, 2)
     }
 }
 
-template <typename T, int V> constexpr int kPairMinBlocks = sizeof(T) == 4 ? 3 : 1;
+// float32: residency for the latency-bound loads (V = 2 needs the registers
+// of its four-row batches: two CTAs per SM)
+template <typename T, int V> constexpr int kPairMinBlocks = sizeof(T) == 4 ? (V == 2 ? 2 : 3) : 1;
 
 // only_if: when not null, the launch is the float64 recomputation after the
 // df64 kernel and returns at once unless *only_if is set.
@@ -278,30 +303,52 @@ __global__ void __launch_bounds__(256, kPairMinBlocks<T, V>)
 #pragma unroll
                 for (int v = 0; v < V; ++v)
                     sre[c][v] = sim[c][v] = T(0);
-#pragma unroll 4
-            for (int m2 = 0; m2 < n_rows; ++m2)
+            // four visited rows at a time, all loads issued before any use
+            // (L2-latency bound); n_rows is 8, 16 or 32
+            for (int m0 = 0; m0 < n_rows; m0 += 4)
             {
-                uint32_t r0 = (uint32_t)m2;
-                if (e1 >= 0)
-                    r0 = ((r0 >> e1) << (e1 + 1)) | (r0 & ((1u << e1) - 1u));
-                if (e2 >= 0)
-                    r0 = ((r0 >> e2) << (e2 + 1)) | (r0 & ((1u << e2) - 1u));
-                if ((int)r0 < RB)
+                uint32_t r0[4];
+                bool ok[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
                 {
-                    T ar[V], ai[V], br[V], bi[V];
-                    load_cvec<T, V>(psi + 2 * ((int64_t)(base + r0) * S + t0), ar, ai);
-                    load_cvec<T, V>(psi + 2 * ((int64_t)(baseB + (r0 ^ xl)) * S + t0), br, bi);
-                    if (split_in_block)
-                    {
-                        // r1 = r0 | 2^a < RB as a < n
-                        const uint32_t r1 = r0 | (1u << abit);
-                        T cr[V], ci[V], dr[V], di[V];
-                        load_cvec<T, V>(psi + 2 * ((int64_t)(base + r1) * S + t0), cr, ci);
-                        load_cvec<T, V>(psi + 2 * ((int64_t)(baseB + (r1 ^ xl)) * S + t0), dr, di);
-                        fma_pair<T, V>(cr, ci, dr, di, sre[1], sim[1]);
-                    }
-                    fma_pair<T, V>(ar, ai, br, bi, sre[0], sim[0]);
+                    uint32_t r = (uint32_t)(m0 + u);
+                    if (e1 >= 0)
+                        r = ((r >> e1) << (e1 + 1)) | (r & ((1u << e1) - 1u));
+                    if (e2 >= 0)
+                        r = ((r >> e2) << (e2 + 1)) | (r & ((1u << e2) - 1u));
+                    r0[u] = r;
+                    ok[u] = (int)r < RB;
                 }
+                T ar[4][V], ai[4][V], br[4][V], bi[4][V];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (ok[u])
+                    {
+                        load_cvec<T, V>(psi + 2 * ((int64_t)(base + r0[u]) * S + t0), ar[u], ai[u]);
+                        load_cvec<T, V>(psi + 2 * ((int64_t)(baseB + (r0[u] ^ xl)) * S + t0), br[u], bi[u]);
+                    }
+                if (split_in_block)
+                {
+                    // rows r1 = r0 | 2^a (< RB as a < n)
+                    T cr[4][V], ci[4][V], dr[4][V], di[4][V];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (ok[u])
+                        {
+                            const uint32_t r1 = r0[u] | (1u << abit);
+                            load_cvec<T, V>(psi + 2 * ((int64_t)(base + r1) * S + t0), cr[u], ci[u]);
+                            load_cvec<T, V>(psi + 2 * ((int64_t)(baseB + (r1 ^ xl)) * S + t0), dr[u], di[u]);
+                        }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (ok[u])
+                            fma_pair<T, V>(cr[u], ci[u], dr[u], di[u], sre[1], sim[1]);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (ok[u])
+                        fma_pair<T, V>(ar[u], ai[u], br[u], bi[u], sre[0], sim[0]);
             }
             // block sums into the running sums: bit a of the block base picks
             // the accumulator when a >= 5

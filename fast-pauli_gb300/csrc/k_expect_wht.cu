@@ -14,7 +14,7 @@
 // which is what makes large groups (e.g. the 105 Z-type strings of a
 // weight <= 2 set) cheap.
 //
-// CTA: 128 threads = TC column lanes x TR row lanes.  A round: every row lane
+// CTA: kWhtThreads = TC column lanes x TR row lanes.  A round: every row lane
 // transforms one 16-row block (both parts, Re and Im, when the chunk has
 // strings of both #Y parities) into shared memory; after a barrier each
 // thread sums, for its own strings (string k belongs to row lane k % TR), the
@@ -214,8 +214,10 @@ template <typename W> __device__ __forceinline__ void wht16(typename W::val (&v)
 
 // only_if: when not null, the float64 recomputation returns at once unless
 // *only_if is set.
-template <typename W, int SLOTS>
-__global__ void __launch_bounds__(128)
+// BOTH: some chunk of the launch has strings of both #Y parities (two
+// transforms per block); otherwise one.
+template <typename W, int SLOTS, bool BOTH>
+__global__ void __launch_bounds__(kWhtThreads)
     k_expect_wht(const typename W::in_t *__restrict__ psi, int64_t S, int n, const StringRec *__restrict__ recs,
                  const int32_t *__restrict__ orig, int64_t P, const WhtChunk *__restrict__ chunks, int TC,
                  int n_splits, double *__restrict__ out, const int *__restrict__ only_if)
@@ -263,42 +265,63 @@ __global__ void __launch_bounds__(128)
     for (int64_t mr = b0; mr < b1; mr += TR)
     {
         const int64_t m = mr + tr;
-        val vre[16], vim[16];
-#pragma unroll
-        for (int r = 0; r < 16; ++r)
-        {
-            vre[r] = W::zero();
-            vim[r] = W::zero();
-        }
         uint64_t base = ~0ull;
-        if (m < b1)
+        const bool have = m < b1;
+        if (have)
         {
             const uint64_t um = (uint64_t)m;
             const uint64_t beta = paired ? (((um >> hb) << (hb + 1)) | (um & ((1ull << hb) - 1ull))) : um;
             base = beta << 4;
-            if (col_ok)
+        }
+        const uint64_t baseB = base ^ xh;
+        cell *w0 = wsm + (size_t)(tr * 16) * TC + tc;        // part 0 (Re)
+        cell *w1 = wsm + (size_t)((TR + tr) * 16) * TC + tc; // part 1 (Im)
+        if constexpr (BOTH)
+        {
+            val vre[16], vim[16];
+#pragma unroll
+            for (int r = 0; r < 16; ++r)
             {
-                const uint64_t baseB = base ^ xh;
+                vre[r] = W::zero();
+                vim[r] = W::zero();
+            }
+            if (have && col_ok)
 #pragma unroll
                 for (int r = 0; r < 16; ++r)
                     if (r < RB)
                         W::q(psi, (int64_t)(base + r) * S + t0, (int64_t)(baseB + (uint64_t)(r ^ xl)) * S + t0, need_re,
                              need_im, vre[r], vim[r]);
+            if (need_re)
+                wht16<W>(vre);
+            if (need_im)
+                wht16<W>(vim);
+#pragma unroll
+            for (int u = 0; u < 16; ++u)
+            {
+                if (need_re)
+                    w0[u * TC] = W::to_cell(vre[u]);
+                if (need_im)
+                    w1[u * TC] = W::to_cell(vim[u]);
             }
         }
-        if (need_re)
-            wht16<W>(vre);
-        if (need_im)
-            wht16<W>(vim);
-        cell *w0 = wsm + (size_t)(tr * 16) * TC + tc;        // part 0 (Re)
-        cell *w1 = wsm + (size_t)((TR + tr) * 16) * TC + tc; // part 1 (Im)
-#pragma unroll
-        for (int u = 0; u < 16; ++u)
+        else
         {
-            if (need_re)
-                w0[u * TC] = W::to_cell(vre[u]);
-            if (need_im)
-                w1[u * TC] = W::to_cell(vim[u]);
+            // every string of the chunk reads the same part: one transform
+            val v[16];
+#pragma unroll
+            for (int r = 0; r < 16; ++r)
+                v[r] = W::zero();
+            if (have && col_ok)
+#pragma unroll
+                for (int r = 0; r < 16; ++r)
+                    if (r < RB)
+                        W::q(psi, (int64_t)(base + r) * S + t0, (int64_t)(baseB + (uint64_t)(r ^ xl)) * S + t0, need_re,
+                             need_im, v[r], v[r]);
+            wht16<W>(v);
+            cell *w = need_re ? w0 : w1;
+#pragma unroll
+            for (int u = 0; u < 16; ++u)
+                w[u * TC] = W::to_cell(v[u]);
         }
         if (tc == 0)
             s_base[tr] = base;
@@ -336,54 +359,69 @@ __global__ void __launch_bounds__(128)
     }
 }
 
-template <typename W, int SL>
+template <typename W, int SL, bool BOTH>
 cudaError_t launch_w(const void *psi, int64_t S, int n, const DevOp &op, const WhtChunk *d_chunks, int n_chunks,
                      int TC, int n_ctiles, int n_splits, double *out, const int *only_if, size_t smem, cudaStream_t st)
 {
     dim3 grid((unsigned)n_chunks, (unsigned)n_splits, (unsigned)n_ctiles);
-    k_expect_wht<W, SL><<<grid, 128, smem, st>>>((const typename W::in_t *)psi, S, n, op.recs, op.orig, op.P,
-                                                 d_chunks, TC, n_splits, out, only_if);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_expect_wht<W, SL, BOTH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    k_expect_wht<W, SL, BOTH><<<grid, kWhtThreads, smem, st>>>((const typename W::in_t *)psi, S, n, op.recs, op.orig,
+                                                               op.P, d_chunks, TC, n_splits, out, only_if);
     return launched();
 }
 
-template <int SL>
+template <int SL, bool BOTH>
 cudaError_t launch_sl(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const WhtChunk *d_chunks,
                       int n_chunks, int TC, int n_ctiles, int n_splits, double *out, int *range_flag,
                       const void *psi_df, size_t smem, cudaStream_t st)
 {
     if (fp32)
-        return launch_w<W32, SL>(psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, nullptr, smem, st);
+        return launch_w<W32, SL, BOTH>(psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, nullptr, smem,
+                                       st);
     if (psi_df)
     {
-        if (cudaError_t e = launch_w<WDF, SL>(psi_df, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out,
-                                              nullptr, smem, st))
+        if (cudaError_t e = launch_w<WDF, SL, BOTH>(psi_df, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out,
+                                                    nullptr, smem, st))
             return e;
-        return launch_w<W64, SL>(psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, range_flag, smem,
-                                 st);
+        return launch_w<W64, SL, BOTH>(psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, range_flag,
+                                       smem, st);
     }
     // no df64 copy of the state: float64 throughout
-    return launch_w<W64, SL>(psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, nullptr, smem, st);
+    return launch_w<W64, SL, BOTH>(psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, nullptr, smem, st);
 }
 
 } // namespace
 
 cudaError_t launch_expect_wht(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const WhtChunk *d_chunks,
-                              int n_chunks, int max_count, int TC, int n_ctiles, int n_splits, double *out,
-                              int *range_flag, const void *psi_df, cudaStream_t st)
+                              int n_chunks, int max_count, bool both_parts, int TC, int n_ctiles, int n_splits,
+                              double *out, int *range_flag, const void *psi_df, cudaStream_t st)
 {
     if (n_chunks <= 0)
         return cudaSuccess;
-    const int threads = 128;
+    const int threads = kWhtThreads;
     const int TR = threads / TC;
     const int slots_needed = (max_count + TR - 1) / TR;
     const size_t smem = (size_t)2 * TR * 16 * TC * 8 + (size_t)TR * 8 + (size_t)max_count * 8;
+#define FPG_WHT(SL, BOTH)                                                                                              \
+    return launch_sl<SL, BOTH>(fp32, psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, range_flag,     \
+                               psi_df, smem, st)
     if (slots_needed <= 8)
-        return launch_sl<8>(fp32, psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, range_flag, psi_df,
-                            smem, st);
-    if (slots_needed <= 32)
-        return launch_sl<32>(fp32, psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, range_flag, psi_df,
-                             smem, st);
-    return cudaErrorInvalidValue;
+    {
+        if (both_parts)
+            FPG_WHT(8, true);
+        FPG_WHT(8, false);
+    }
+    if (slots_needed <= 16)
+    {
+        if (both_parts)
+            FPG_WHT(16, true);
+        FPG_WHT(16, false);
+    }
+#undef FPG_WHT
+    return cudaErrorInvalidValue; // TR >= 8 and <= kWhtMaxStrings strings: at most 16 slots
 }
 
 } // namespace fpg
