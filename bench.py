@@ -474,6 +474,52 @@ def _cfg4_problems(seed=1004, count=256):
     return probs
 
 
+def run_to_tensor(args):
+    """SummedPauliOp.to_tensor: n=12, the 703 weight<=2 strings (identity
+    excluded), K=8 operators -> (8, 4096, 4096) complex128 (2.1 GB).  Metric:
+    string-rows/s = P * 2^n * K per call (the reference visits each)."""
+    import numpy as np
+    import torch
+
+    import oracle
+    from fast_pauli import _abi
+
+    torch.cuda.set_device(0)
+    n, K = 12, 8
+    strings, h, _ = config2(n=n, K=K, S=1, seed=1007)
+    P, D = len(strings), 1 << n
+    L = _abi.lib()
+    op = _abi.Operator(strings)
+    stream = _stream_handle()
+    dh = torch.from_numpy(h).cuda()
+    out = torch.zeros((K, D, D), dtype=torch.complex128, device="cuda")
+
+    def step():
+        _abi.check(L.fpg_to_tensor(op.handle, dh.data_ptr(), K, out.data_ptr(), _abi.FPG_C128, stream))
+
+    t = time_device(step, args.steps, args.warmup)
+    units = P * D * K
+    # parity on a slice: one operator, against the oracle restatement
+    out.zero_()
+    step()
+    torch.cuda.synchronize()
+    want0 = oracle.summed_to_tensor(strings[:50], h[:50, :1])
+    o2 = torch.zeros((1, D, D), dtype=torch.complex128, device="cuda")
+    op2 = _abi.Operator(strings[:50])
+    dh2 = torch.from_numpy(np.ascontiguousarray(h[:50, :1])).cuda()
+    _abi.check(L.fpg_to_tensor(op2.handle, dh2.data_ptr(), 1, o2.data_ptr(), _abi.FPG_C128, stream))
+    err = float(np.abs(o2.cpu().numpy() - want0).max() / np.abs(want0).max())
+    tc = time.perf_counter()
+    oracle.summed_to_tensor(strings, h[:, :2])
+    tc = time.perf_counter() - tc
+    return {"metric": "to_tensor string-rows/s", "value": units / t, "unit": "string-rows/s",
+            "workload": f"SummedPauliOp.to_tensor float64: n={n}, {P} weight<=2 strings, K={K} -> ({K}, {D}, {D})",
+            "ms_per_step": t * 1e3, "steps": args.steps, "warmup": args.warmup,
+            "rmw_bytes_per_step": P * D * K * 32, "max_normwise_err_vs_oracle_50_strings": err,
+            "cpu_baseline": {"value": P * D * 2 / tc, "unit": "string-rows/s", "cores": oracle.max_threads(),
+                             "kind": "port", "sample": f"all {P} strings, 2 of {K} operators ({tc:.2f} s)"}}
+
+
 def run_square(args):
     """SummedPauliOp.square of the configuration-2 operator set (n=14, 861
     weight<=2 strings, K=1000) onto the 91771 strings of weight <= 4.
@@ -744,7 +790,7 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-mixed", action="store_true")
-    ap.add_argument("--workload", default="summed", choices=["summed", "batch", "serve", "square"],
+    ap.add_argument("--workload", default="summed", choices=["summed", "batch", "serve", "square", "to_tensor"],
                     help="summed: configuration 2 (default line); batch: configuration 4; serve: configuration 5; "
                          "square: SummedPauliOp.square of the configuration-2 operators")
     ap.add_argument("--requests", type=int, default=60, help="serve: requests per rate")
@@ -762,7 +808,8 @@ def main():
         return
     if args.workload != "summed" and args.impl == "ours":
         if rank == 0:
-            line = {"batch": run_batch, "serve": run_serve, "square": run_square}[args.workload](args)
+            line = {"batch": run_batch, "serve": run_serve, "square": run_square,
+                    "to_tensor": run_to_tensor}[args.workload](args)
             print(json.dumps(line), flush=True)
         return
     if args.impl == "reference":

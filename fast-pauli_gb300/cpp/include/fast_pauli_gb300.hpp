@@ -886,18 +886,22 @@ template <std::floating_point T, typename H = std::complex<T>> struct PauliOp
         run_expect(expectation_vals_out.data_handle(), states.data_handle(), S, false);
     }
 
+    // Dense matrix, accumulated into output (reference :558-571), on the GPU
+    // (fpg_to_tensor).
     template <typename View> void to_tensor(View output) const
     {
         using C = detail::elem_t<View>;
-        C *o = output.data_handle();
-        const size_t D = dim();
-        for (size_t i = 0; i < pauli_strings.size(); ++i)
-        {
-            auto [k, m] = get_sparse_repr<typename C::value_type>(pauli_strings[i].paulis);
-            const C c = C(coeffs[i]);
-            for (size_t j = 0; j < D; ++j)
-                o[j * D + k[j]] += c * m[j];
-        }
+        if (pauli_strings.empty() || dim() == 0)
+            return;
+        fpg_operator *op = cache_.get(pauli_strings);
+        cudaStream_t st = detail::stream();
+        detail::Staged o(output.data_handle(), dim() * dim() * sizeof(C), 1, st);
+        std::vector<C> c(coeffs.begin(), coeffs.end());
+        detail::DevBuf dc(c.size() * sizeof(C), st);
+        detail::cuda_check(cudaMemcpyAsync(dc.p, c.data(), dc.bytes, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
+        detail::check(fpg_to_tensor(op, dc.p, 1, o.dev(), detail::dtype_of<C>(), st));
+        o.finish();
+        detail::finish_call(st, {&o});
     }
 
     static inline void validate_pauli_strings(std::vector<PauliString> const &ps)
@@ -1112,18 +1116,21 @@ template <std::floating_point T> struct SummedPauliOp
         return SummedPauliOp(sq, Tensor<2>(out.data(), A, K));
     }
 
+    // Dense matrices (K, D, D), accumulated into A_k_out (reference :644-665),
+    // on the GPU (fpg_to_tensor).
     template <typename View> void to_tensor(View A_k_out) const
     {
         using C = detail::elem_t<View>;
-        C *o = A_k_out.data_handle();
-        const size_t D = dim();
-        for (size_t i = 0; i < pauli_strings.size(); ++i)
-        {
-            auto [cols, vals] = get_sparse_repr<typename C::value_type>(pauli_strings[i].paulis);
-            for (size_t k = 0; k < n_operators(); ++k)
-                for (size_t j = 0; j < D; ++j)
-                    o[(k * D + j) * D + cols[j]] += C(coeffs(i, k)) * vals[j];
-        }
+        const size_t D = dim(), K = n_operators();
+        if (pauli_strings.empty() || D == 0 || K == 0)
+            return;
+        fpg_operator *op = cache_.get(pauli_strings);
+        cudaStream_t st = detail::stream();
+        detail::Staged o(A_k_out.data_handle(), K * D * D * sizeof(C), 1, st);
+        detail::DevBuf dh = upload_coeffs<C>(st);
+        detail::check(fpg_to_tensor(op, dh.p, (int64_t)K, o.dev(), detail::dtype_of<C>(), st));
+        o.finish();
+        detail::finish_call(st, {&o});
     }
 
     // Internal entry points used by the bindings.

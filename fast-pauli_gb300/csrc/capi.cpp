@@ -898,6 +898,30 @@ extern "C"
         return FPG_OK;
     }
 
+    int fpg_to_tensor(const fpg_operator *op, const void *coeffs, int64_t n_operators, void *out, int32_t dtype,
+                      void *stream)
+    {
+        if (!op)
+            return set_error(FPG_ERR_INVALID, "op is null");
+        if (int rc = check_dtype(dtype))
+            return rc;
+        if (n_operators < 0)
+            return set_error(FPG_ERR_INVALID, "n_operators must be >= 0");
+        if (n_operators == 0 || op->P == 0)
+            return FPG_OK;
+        if (!coeffs || !out)
+            return set_error(FPG_ERR_INVALID, "null array");
+        if (int rc = check_aligned(dtype, {coeffs, out}))
+            return rc;
+        if (op->n > 24)
+            return set_error(FPG_ERR_UNSUPPORTED, "to_tensor: 2^n x 2^n matrices only up to n = 24");
+        DeviceGuard g(op->device);
+        if (!g.ok)
+            return set_error(FPG_ERR_CUDA, "cannot select the operator's device");
+        FPG_CUDA(launch_to_tensor(dtype == FPG_C64, op->dev(), coeffs, n_operators, out, (cudaStream_t)stream));
+        return FPG_OK;
+    }
+
     int fpg_summed_square(const fpg_operator *op, const void *coeffs, int64_t n_operators, const fpg_operator *sq,
                           void *out, int32_t dtype, void *stream)
     {

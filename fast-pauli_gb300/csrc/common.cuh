@@ -266,6 +266,10 @@ size_t square_workspace_bytes(int64_t P, int64_t A);
 cudaError_t launch_square(bool fp32, const DevOp &op, const DevOp &sq, const void *h, int64_t K, void *out,
                           void *ws, unsigned long long **found, cudaStream_t st);
 
+// out(k, i, j) += (sum_j coeffs(j,k) P_j)(i, j): the dense matrices of K
+// operators, out (K, 2^n, 2^n) complex.
+cudaError_t launch_to_tensor(bool fp32, const DevOp &op, const void *coeffs, int64_t K, void *out, cudaStream_t st);
+
 cudaError_t launch_sparse_repr(uint64_t x, uint64_t z, int ny, int n, uint64_t *cols, void *vals, cudaStream_t st);
 
 } // namespace fpg

@@ -84,6 +84,8 @@ __global__ void k_prep_weighted(const StringRec *__restrict__ recs, const int32_
     }
 }
 
+constexpr int kApplyRows = 8; // output rows per thread
+
 template <typename T, bool WEIGHTED>
 __global__ void __launch_bounds__(256)
     k_apply(const T *__restrict__ psi, T *__restrict__ out, int64_t S, int n, const Group *__restrict__ groups,
@@ -95,43 +97,108 @@ __global__ void __launch_bounds__(256)
     const int tr = tid / TC;
     const int TR = blockDim.x / TC;
     const uint64_t D = 1ull << n;
-    const uint64_t i = (uint64_t)blockIdx.x * TR + tr;
+    // R consecutive rows per thread: the coefficients of a string (per column
+    // for apply_weighted) are loaded once for all of them, and their partner
+    // rows i ^ x_g lie side by side (R loads in flight per group)
+    const uint64_t i0 = ((uint64_t)blockIdx.x * TR + tr) * kApplyRows;
     const int64_t t = (int64_t)blockIdx.y * TC + tc;
-    if (i >= D || t >= S)
+    if (i0 >= D || t >= S)
         return;
     const CT *ps = reinterpret_cast<const CT *>(psi);
-    T accr = 0, acci = 0;
+    T accr[kApplyRows], acci[kApplyRows];
+#pragma unroll
+    for (int k = 0; k < kApplyRows; ++k)
+        accr[k] = acci[k] = T(0);
     // groups in order, one at a time: every warp then sweeps the partner rows
     // i ^ x_g in step with its neighbours (loading several groups ahead per
     // thread measured 3x slower on large states: it scatters the reads)
     for (int64_t g = 0; g < G; ++g)
     {
         const Group gr = groups[g];
-        T wr = 0, wi = 0;
+        CT b[kApplyRows];
+#pragma unroll
+        for (int k = 0; k < kApplyRows; ++k)
+            if (i0 + k < D)
+                b[k] = __ldg(ps + (int64_t)((i0 + k) ^ gr.x) * S + t);
+        T wr[kApplyRows], wi[kApplyRows];
+#pragma unroll
+        for (int k = 0; k < kApplyRows; ++k)
+            wr[k] = wi[k] = T(0);
         for (int32_t s = gr.begin; s < gr.begin + gr.count; ++s)
         {
             const uint64_t z = recs[s].z;
             const CT c = WEIGHTED ? cw[(int64_t)s * S + t] : cw[s];
-            if (__popcll(i & z) & 1)
+#pragma unroll
+            for (int k = 0; k < kApplyRows; ++k)
             {
-                wr -= c.x;
-                wi -= c.y;
-            }
-            else
-            {
-                wr += c.x;
-                wi += c.y;
+                if (__popcll((i0 + k) & z) & 1)
+                {
+                    wr[k] -= c.x;
+                    wi[k] -= c.y;
+                }
+                else
+                {
+                    wr[k] += c.x;
+                    wi[k] += c.y;
+                }
             }
         }
-        const CT b = __ldg(ps + (int64_t)(i ^ gr.x) * S + t);
-        accr = fma(wr, b.x, fma(-wi, b.y, accr));
-        acci = fma(wr, b.y, fma(wi, b.x, acci));
+#pragma unroll
+        for (int k = 0; k < kApplyRows; ++k)
+            if (i0 + k < D)
+            {
+                accr[k] = fma(wr[k], b[k].x, fma(-wi[k], b[k].y, accr[k]));
+                acci[k] = fma(wr[k], b[k].y, fma(wi[k], b[k].x, acci[k]));
+            }
     }
-    CT *o = reinterpret_cast<CT *>(out) + (int64_t)i * S + t;
-    CT cur = *o;
-    cur.x += accr;
-    cur.y += acci;
-    *o = cur;
+#pragma unroll
+    for (int k = 0; k < kApplyRows; ++k)
+        if (i0 + k < D)
+        {
+            CT *o = reinterpret_cast<CT *>(out) + (int64_t)(i0 + k) * S + t;
+            CT cur = *o;
+            cur.x += accr[k];
+            cur.y += acci[k];
+            *o = cur;
+        }
+}
+
+// out(k, i, i ^ x_g) += sum_{s in g} coeffs(orig[s], k) (-i)^nY_s (-1)^popc(i & z_s)
+// for every operator k, row i and x-group g: each output element belongs to
+// one (k, i, g), so the additions need no atomics.
+template <typename CT>
+__global__ void k_to_tensor(const StringRec *__restrict__ recs, const int32_t *__restrict__ orig,
+                            const Group *__restrict__ groups, int64_t G, const CT *__restrict__ coeffs, int64_t K,
+                            int n, CT *__restrict__ out)
+{
+    const uint64_t D = 1ull << n;
+    const uint64_t total = (uint64_t)K * D * (uint64_t)G;
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (uint64_t)gridDim.x * blockDim.x)
+    {
+        const uint64_t i = e % D; // rows fastest: consecutive threads write neighbouring rows
+        const uint64_t rest = e / D;
+        const int64_t g = (int64_t)(rest % (uint64_t)G);
+        const int64_t k = (int64_t)(rest / (uint64_t)G);
+        const Group gr = groups[g];
+        CT v;
+        v.x = 0;
+        v.y = 0;
+        for (int32_t s = gr.begin; s < gr.begin + gr.count; ++s)
+        {
+            CT c = times_phase(coeffs[(int64_t)orig[s] * K + k], (int)(recs[s].meta & 3u));
+            if (__popcll(i & recs[s].z) & 1)
+            {
+                c.x = -c.x;
+                c.y = -c.y;
+            }
+            v.x += c.x;
+            v.y += c.y;
+        }
+        CT &dst = out[((uint64_t)k * D + i) * D + (i ^ gr.x)];
+        dst.x += v.x;
+        dst.y += v.y;
+    }
 }
 
 __global__ void k_sparse_repr(uint64_t x, uint64_t z, int ny, uint64_t D, uint64_t *__restrict__ cols,
@@ -193,7 +260,8 @@ cudaError_t launch_apply(bool fp32, bool weighted, const DevOp &op, const void *
     const int TC = pick_tc(S);
     const int TR = 256 / TC;
     const uint64_t D = 1ull << op.n;
-    dim3 grid((unsigned)((D + TR - 1) / TR), (unsigned)((S + TC - 1) / TC));
+    const uint64_t rows_per_cta = (uint64_t)TR * kApplyRows;
+    dim3 grid((unsigned)((D + rows_per_cta - 1) / rows_per_cta), (unsigned)((S + TC - 1) / TC));
     if (fp32)
     {
         if (weighted)
@@ -212,6 +280,23 @@ cudaError_t launch_apply(bool fp32, bool weighted, const DevOp &op, const void *
             k_apply<double, false><<<grid, 256, 0, st>>>((const double *)psi, (double *)out, S, op.n, op.groups,
                                                          op.G, op.recs, (const double2 *)cw, TC);
     }
+    return launched();
+}
+
+cudaError_t launch_to_tensor(bool fp32, const DevOp &op, const void *coeffs, int64_t K, void *out, cudaStream_t st)
+{
+    if (K <= 0 || op.G <= 0)
+        return cudaSuccess;
+    const uint64_t total = (uint64_t)K * (1ull << op.n) * (uint64_t)op.G;
+    uint64_t blocks = (total + 255) / 256;
+    if (blocks > 152 * 32)
+        blocks = 152 * 32;
+    if (fp32)
+        k_to_tensor<float2><<<(unsigned)blocks, 256, 0, st>>>(op.recs, op.orig, op.groups, op.G,
+                                                              (const float2 *)coeffs, K, op.n, (float2 *)out);
+    else
+        k_to_tensor<double2><<<(unsigned)blocks, 256, 0, st>>>(op.recs, op.orig, op.groups, op.G,
+                                                               (const double2 *)coeffs, K, op.n, (double2 *)out);
     return launched();
 }
 

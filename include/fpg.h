@@ -169,6 +169,16 @@ int fpg_summed_apply_weighted(const fpg_operator *op, const void *coeffs, int64_
 int fpg_summed_square(const fpg_operator *op, const void *coeffs, int64_t n_operators, const fpg_operator *sq,
                       void *out, int32_t dtype, void *stream);
 
+/*
+ * Dense matrices of the operators A_k = sum_j coeffs(j,k) P_j:
+ *   out(k, i, j) += A_k(i, j),   out (K, 2^n, 2^n) complex, coeffs (n_strings, K),
+ * both device arrays of dtype.  Outputs accumulate, as in the reference.
+ * Replaces SummedPauliOp::to_tensor (__summed_pauli_op.hpp:644-665) and, with
+ * K = 1, PauliOp::to_tensor (__pauli_op.hpp:558-571).
+ */
+int fpg_to_tensor(const fpg_operator *op, const void *coeffs, int64_t n_operators, void *out, int32_t dtype,
+                  void *stream);
+
 /* ------------------------------------------------------------------------
  * Batches: many expectation problems of uneven size (qubits, strings,
  * states, operators) run as one persistent work-queue launch per chunk class

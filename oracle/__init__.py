@@ -72,6 +72,7 @@ def lib() -> ctypes.CDLL:
         L.fpo_summed_apply_weighted.argtypes = [P, i64, ci, P, i64, i64, P, P, P]
         L.fpo_summed_square.argtypes = [P, i64, ci, P, i64, P, i64, P]
         L.fpo_summed_square.restype = ci
+        L.fpo_summed_to_tensor.argtypes = [P, i64, ci, P, i64, P]
         L.fpo_max_threads.restype = ci
         _lib = L
     return _lib
@@ -233,6 +234,16 @@ def summed_apply_weighted(strings, h, psi, data) -> np.ndarray:
         _p(codes), len(strings), n, _p(h), h.shape[1], p2.shape[1], _p(p2), _p(d2), _p(out)
     )
     return out.reshape(psi.shape)
+
+
+def summed_to_tensor(strings, h) -> np.ndarray:
+    """Dense matrices (K, 2^n, 2^n) of the operators sum_j h(j,k) P_j."""
+    codes, n = codes_of(strings)
+    h = _c(h)
+    K = h.shape[1]
+    out = np.zeros((K, 1 << n, 1 << n), dtype=np.complex128)
+    lib().fpo_summed_to_tensor(_p(codes), len(strings), n, _p(h), K, _p(out))
+    return out
 
 
 def summed_square(strings, h, sq_strings) -> np.ndarray:

@@ -448,6 +448,38 @@ int fpo_summed_square(const uint8_t *codes, int64_t P, int n, const double *h, i
     return missing ? -1 : 0;
 }
 
+/*
+ * fpo_summed_to_tensor <- SummedPauliOp::to_tensor (__summed_pauli_op.hpp:644-665):
+ * out (K, D, D) complex, accumulated: for every string its sparse pattern,
+ * then out(k, j, cols[j]) += h(i, k) * vals[j], strings in order, OpenMP over
+ * the operators k.
+ */
+void fpo_summed_to_tensor(const uint8_t *codes, int64_t P, int n, const double *h, int64_t K, double *out)
+{
+    const uint64_t D = (uint64_t)1 << n;
+    uint64_t *cols = (uint64_t *)malloc(D * sizeof(uint64_t));
+    double *vals = (double *)malloc(D * 2 * sizeof(double));
+    for (int64_t i = 0; i < P; ++i)
+    {
+        fpo_sparse_repr(codes + i * n, n, cols, vals);
+#pragma omp parallel for schedule(static)
+        for (int64_t k = 0; k < K; ++k)
+        {
+            const double cr = h[2 * (i * K + k)], ci = h[2 * (i * K + k) + 1];
+            for (uint64_t j = 0; j < D; ++j)
+            {
+                double vr, vi;
+                cmul(cr, ci, vals[2 * j], vals[2 * j + 1], &vr, &vi);
+                double *o = out + 2 * (((uint64_t)k * D + j) * D + cols[j]);
+                o[0] += vr;
+                o[1] += vi;
+            }
+        }
+    }
+    free(vals);
+    free(cols);
+}
+
 int fpo_max_threads(void)
 {
     return max_threads();

@@ -290,6 +290,33 @@ def test_to_tensor_matches_dense():
     np.testing.assert_allclose(t[1], 2 * want, atol=1e-13)
 
 
+@pytest.mark.parametrize("n,P,K", [(1, 3, 1), (4, 20, 3), (7, 60, 2)])
+def test_to_tensor_device_vs_dense_and_accumulates(n, P, K):
+    """fpg_to_tensor against the kron-built dense matrices (duplicates and
+    identity strings included), accumulating into the output like the
+    reference's to_tensor."""
+    torch = pytest.importorskip("torch")
+    from fast_pauli import _abi
+
+    L = _abi.lib()
+    rng = np.random.default_rng(90 + n)
+    strings = oracle.uniform_strings(rng, n, P)
+    strings[0] = "I" * n
+    strings[-1] = strings[1]
+    h = rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))
+    want = np.stack([sum(h[j, k] * oracle.dense(s) for j, s in enumerate(strings)) for k in range(K)])
+    op = _abi.Operator(strings)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    D = 1 << n
+    for dtype, tdt, tol in ((_abi.FPG_C128, torch.complex128, 1e-13), (_abi.FPG_C64, torch.complex64, 1e-5)):
+        dh = torch.from_numpy(h).to(tdt).cuda()
+        out = torch.ones((K, D, D), dtype=tdt, device="cuda")
+        _abi.check(L.fpg_to_tensor(op.handle, dh.data_ptr(), K, out.data_ptr(), dtype, st))
+        torch.cuda.synchronize()
+        assert normwise(out.cpu().numpy() - 1.0, want) < tol, dtype
+    op.close()
+
+
 # ------------------------------------------------------------ device tensors
 
 

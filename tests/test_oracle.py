@@ -84,6 +84,14 @@ def test_summed_square_golden(name):
     assert [str(x) for x in g["sq_strings"]] == oracle.calculate_pauli_strings_max_weight(n, min(n, 2 * w))
 
 
+def test_summed_to_tensor_matches_dense_kron():
+    rng = np.random.default_rng(12)
+    strings = oracle.uniform_strings(rng, 4, 9) + ["IIII"]
+    h = rng.standard_normal((10, 3)) + 1j * rng.standard_normal((10, 3))
+    want = np.stack([sum(h[j, k] * oracle.dense(s) for j, s in enumerate(strings)) for k in range(3)])
+    assert normwise(oracle.summed_to_tensor(strings, h), want) < 1e-15
+
+
 def test_summed_square_missing_product_is_reported():
     with pytest.raises(ValueError):
         oracle.summed_square(["XI", "IZ"], np.ones((2, 1)), ["II", "XI", "IZ"])  # XZ missing
