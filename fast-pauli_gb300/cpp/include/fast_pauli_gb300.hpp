@@ -141,8 +141,9 @@ inline bool on_device(const void *p)
     return d != 0;
 }
 
-// Stream-ordered device buffer (cudaMallocAsync), freed stream-ordered on
-// scope exit, so temporaries never force a device-wide synchronisation.
+// Stream-ordered device buffer from the library's pool (fpg_device_alloc),
+// freed stream-ordered on scope exit, so temporaries never force a
+// device-wide synchronisation and stay mapped for the next call.
 struct DevBuf
 {
     void *p = nullptr;
@@ -152,7 +153,7 @@ struct DevBuf
     DevBuf(size_t n, cudaStream_t s) : bytes(n), st(s)
     {
         if (n)
-            cuda_check(cudaMallocAsync(&p, n, s), "cudaMallocAsync");
+            check(fpg_device_alloc(&p, n, s));
     }
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
@@ -163,7 +164,7 @@ struct DevBuf
     ~DevBuf()
     {
         if (p)
-            cudaFreeAsync(p, st);
+            fpg_device_free(p, st);
     }
 };
 
@@ -273,6 +274,13 @@ struct OpHandle
 };
 
 } // namespace detail
+
+// Return the library pool's unused device memory (temporaries of earlier
+// calls, kept mapped for reuse) to the device.
+inline void release_cached_memory()
+{
+    detail::check(fpg_release_cached_memory());
+}
 
 // ---------------------------------------------------------------------------
 // Pauli (reference: __pauli.hpp:39-212)

@@ -738,6 +738,9 @@ PYBIND11_MODULE(_fast_pauli, m)
                             return SummedD(t[0].cast<std::vector<fp::PauliString>>(), t[1].cast<std::vector<cd>>());
                         }));
 
+    m.def("release_cached_memory", &fp::release_cached_memory,
+          "Return the device memory the library keeps for reuse by later calls to the device.");
+
     // ----------------------------------------------------------------- helpers
     auto helpers = m.def_submodule("helpers");
     helpers.def("get_nontrivial_paulis", &fp::get_nontrivial_paulis, "weight"_a);

@@ -9,7 +9,9 @@
 #include <atomic>
 #include <initializer_list>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -335,6 +337,67 @@ int check_aligned(int32_t dtype, std::initializer_list<const void *> ptrs)
     return FPG_OK;
 }
 
+// Device memory of the library's temporaries: one stream-ordered pool per
+// device that keeps up to FPG_POOL_KEEP_BYTES (default 4 GiB) mapped across
+// synchronisations.  The device's default pool gives all freed memory back
+// at every synchronisation, so host-buffer calls that synchronise would map
+// and unmap their staging and scratch buffers (hundreds of MB) every time.
+constexpr int kMaxPoolDevices = 64;
+std::mutex g_pool_mu;
+cudaMemPool_t g_pools[kMaxPoolDevices];
+
+uint64_t pool_keep_bytes()
+{
+    const char *e = std::getenv("FPG_POOL_KEEP_BYTES");
+    if (e && *e)
+    {
+        char *end = nullptr;
+        const unsigned long long v = std::strtoull(e, &end, 10);
+        if (end && *end == '\0')
+            return v;
+    }
+    return 4ull << 30;
+}
+
+cudaError_t library_pool(cudaMemPool_t *out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    if (dev < 0 || dev >= kMaxPoolDevices)
+        return cudaDeviceGetDefaultMemPool(out, dev);
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    if (!g_pools[dev])
+    {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t p = nullptr;
+        if ((e = cudaMemPoolCreate(&p, &props)) != cudaSuccess)
+            return e;
+        uint64_t keep = pool_keep_bytes();
+        if ((e = cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep)) != cudaSuccess)
+        {
+            cudaMemPoolDestroy(p);
+            return e;
+        }
+        g_pools[dev] = p;
+    }
+    *out = g_pools[dev];
+    return cudaSuccess;
+}
+
+cudaError_t pool_alloc(void **p, size_t bytes, cudaStream_t st)
+{
+    cudaMemPool_t pool = nullptr;
+    cudaError_t e = library_pool(&pool);
+    if (e != cudaSuccess)
+        return e;
+    return cudaMallocFromPoolAsync(p, bytes ? bytes : 16, pool, st);
+}
+
 // Stream-ordered scratch allocation, freed on scope exit (also stream ordered).
 struct Scratch
 {
@@ -345,7 +408,7 @@ struct Scratch
     }
     cudaError_t alloc(size_t bytes)
     {
-        return cudaMallocAsync(&p, bytes ? bytes : 16, st);
+        return pool_alloc(&p, bytes, st);
     }
     ~Scratch()
     {
@@ -569,6 +632,37 @@ extern "C"
             c = 0;
         }
         *count = c;
+        return FPG_OK;
+    }
+
+    int fpg_device_alloc(void **ptr, size_t bytes, void *stream)
+    {
+        if (!ptr)
+            return set_error(FPG_ERR_INVALID, "ptr is null");
+        *ptr = nullptr;
+        cudaError_t e = pool_alloc(ptr, bytes, (cudaStream_t)stream);
+        if (e == cudaErrorMemoryAllocation)
+        {
+            cudaGetLastError();
+            return set_error(FPG_ERR_NOMEM, "device memory exhausted (" + std::to_string(bytes) + " bytes)");
+        }
+        FPG_CUDA(e);
+        return FPG_OK;
+    }
+
+    int fpg_device_free(void *ptr, void *stream)
+    {
+        if (ptr)
+            FPG_CUDA(cudaFreeAsync(ptr, (cudaStream_t)stream));
+        return FPG_OK;
+    }
+
+    int fpg_release_cached_memory(void)
+    {
+        std::lock_guard<std::mutex> lock(g_pool_mu);
+        for (cudaMemPool_t p : g_pools)
+            if (p)
+                FPG_CUDA(cudaMemPoolTrimTo(p, 0));
         return FPG_OK;
     }
 

@@ -14,6 +14,7 @@ from ._fast_pauli import (  # noqa: F401
     PauliString,
     SummedPauliOp,
     helpers,
+    release_cached_memory,
 )
 
 

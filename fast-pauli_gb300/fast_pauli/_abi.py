@@ -41,6 +41,9 @@ SIGNATURES = {
     "fpg_device_error": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), _P]),
     "fpg_device_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int)]),
     "fpg_pointer_is_device": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
+    "fpg_device_alloc": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_size_t, _P]),
+    "fpg_device_free": (ctypes.c_int, [_P, _P]),
+    "fpg_release_cached_memory": (ctypes.c_int, []),
     "fpg_operator_create": (ctypes.c_int, [ctypes.c_char_p, _I64, _I32, ctypes.POINTER(_P)]),
     "fpg_operator_destroy": (ctypes.c_int, [_P]),
     "fpg_operator_info": (ctypes.c_int, [_P, _PI32, _PI64, _PI64]),

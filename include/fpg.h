@@ -85,6 +85,18 @@ int fpg_device_count(int *count);
 /* 1 if ptr is device (or managed) memory on some device, else 0. */
 int fpg_pointer_is_device(const void *ptr, int *is_device);
 
+/* Stream-ordered device memory from the library's pool on the current
+ * device (the pool the entry points take their scratch from).  Freed memory
+ * stays mapped for reuse up to FPG_POOL_KEEP_BYTES (environment, bytes;
+ * default 4 GiB), so calls that synchronise do not remap their buffers.
+ * bytes = 0 allocates a minimal block.  FPG_ERR_NOMEM when the device is
+ * full.  No reference counterpart: the reference's CPU path allocates with
+ * std::vector per call (__summed_pauli_op.hpp). */
+int fpg_device_alloc(void **ptr, size_t bytes, void *stream);
+int fpg_device_free(void *ptr, void *stream);
+/* Give the pool's unused memory back to the device (all devices). */
+int fpg_release_cached_memory(void);
+
 /*
  * Encode n_strings Pauli strings of n_qubits characters each and upload the
  * encoding to the current device.  Replaces the per-call get_sparse_repr of

@@ -74,3 +74,16 @@ def test_pointer_classification_of_host_memory():
     d = ctypes.c_int(7)
     assert _abi.lib().fpg_pointer_is_device(ctypes.cast(buf, ctypes.c_void_p), ctypes.byref(d)) == 0
     assert d.value == 0
+
+
+def test_memory_pool_entry_points_without_device():
+    from fast_pauli import _abi
+
+    import fast_pauli as fp
+
+    L = _abi.lib()
+    assert L.fpg_device_alloc(None, 16, None) == _abi.FPG_ERR_INVALID
+    assert L.fpg_device_free(None, None) == _abi.FPG_OK
+    # nothing allocated yet in this process: releasing is a no-op
+    assert L.fpg_release_cached_memory() == _abi.FPG_OK
+    assert fp.release_cached_memory() is None

@@ -104,6 +104,24 @@ def test_weight2_strings_summed_expectation(n, S):
     assert normwise(got, oracle.summed_expectation(strings, h, psi)) < TOL_C128
 
 
+def test_pool_memory_reused_and_released():
+    # temporaries come from the library's pool: back-to-back host-buffer
+    # calls (each synchronises) reuse it; after release_cached_memory the
+    # next call maps fresh memory and gives the same result
+    rng = np.random.default_rng(77)
+    n, S = 9, 33
+    strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
+    P, K = len(strings), 4
+    h = (rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))) / np.sqrt(2 * P)
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    sop = fp.SummedPauliOp(strings, h)
+    first = sop.expectation_value(psi)
+    assert normwise(first, oracle.summed_expectation(strings, h, psi)) < TOL_C128
+    np.testing.assert_array_equal(sop.expectation_value(psi), first)
+    fp.release_cached_memory()
+    np.testing.assert_array_equal(sop.expectation_value(psi), first)
+
+
 def _masks_to_string(n, x, z):
     # row bit r <-> character n-1-r
     ch = {(0, 0): "I", (1, 0): "X", (1, 1): "Y", (0, 1): "Z"}
