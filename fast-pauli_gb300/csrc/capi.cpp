@@ -581,8 +581,7 @@ size_t request_scratch_bytes(const fpg_operator *op, int64_t K, int64_t S, bool 
     const int64_t split_bytes = ((int64_t)1 << op->n) * S * 16;
     if (!fp32 && (!op->pairs.empty() || !op->margs.empty() || !op->wht.empty()) && split_bytes <= kDfSplitMaxBytes)
         b += (size_t)split_bytes; // the df64 copy of the state
-    if (fp32)
-        b += tc_workspace_bytes(2 * K, S, op->P);
+    b += fp32 ? tc_workspace_bytes(2 * K, S, op->P) : oz_workspace_bytes(2 * K, S, op->P);
     return b + 4096;
 }
 } // namespace fpg
@@ -887,10 +886,15 @@ extern "C"
                                                ws.p, st));
             return FPG_OK;
         }
-        int *range_flag = (int *)((char *)evb.p + ev_bytes);
-        FPG_CUDA(cudaMemsetAsync(range_flag, 0, sizeof(int), st));
-        FPG_CUDA(launch_contract_real(fp32, coeffs, fp32, (const double *)evb.p, op->P, n_operators, n_states, out,
-                                      range_flag, st));
+        // float64: the contraction on the tensor cores (exact digit-slice
+        // products), or the float64 GEMM when H or E holds a non-finite value
+        int *flag = (int *)((char *)evb.p + ev_bytes);
+        FPG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+        Scratch ws(st);
+        FPG_CUDA(ws.alloc(oz_workspace_bytes(2 * n_operators, n_states, op->P)));
+        FPG_CUDA(launch_contract_oz_expect(coeffs, (const double *)evb.p, op->P, n_operators, n_states, out, ws.p,
+                                           flag, st));
+        FPG_CUDA(launch_contract_f64_if(coeffs, (const double *)evb.p, op->P, n_operators, n_states, out, flag, st));
         return FPG_OK;
     }
 

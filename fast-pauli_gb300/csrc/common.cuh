@@ -217,14 +217,11 @@ cudaError_t launch_expect_wht(bool fp32, const void *psi, int64_t S, int n, cons
                               int n_chunks, int max_count, bool both_parts, int TC, int n_ctiles, int n_splits,
                               double *out, int *range_flag, const void *psi_df, cudaStream_t st);
 
-// out(K,S) += H^T(K,P) * E(P,S); H complex (P,K), E real float64 (P,S).
-// out complex128 (fp32=false) or complex64 (fp32=true).
-// range_flag (complex128 H and out only; a device int, zero before the call):
-// when given, the GEMM runs in df64 on the float32 pipes, or in float64 when
-// some value of H or E lies outside the df64 range (df64.cuh); when null,
-// float64 throughout.
+// out(K,S) += H^T(K,P) * E(P,S); H complex (P,K), E real float64 (P,S),
+// float64 arithmetic on the CUDA cores (the allocation-free entry point's
+// contraction).  out complex128 or complex64 (out_c64).
 cudaError_t launch_contract_real(bool out_c64, const void *H, bool h_c64, const double *E, int64_t P, int64_t K,
-                                 int64_t S, void *out, int *range_flag, cudaStream_t st);
+                                 int64_t S, void *out, cudaStream_t st);
 
 // Tensor-core (tcgen05, 3xTF32, float32 accumulation) forms for the mixed
 // path; ws must hold tc_workspace_bytes(M, N, Kd) of the GEMM they run:
@@ -236,6 +233,19 @@ cudaError_t launch_contract_tc_expect(const void *H, const double *E, int64_t P,
 // W(P,S) complex64 = H X with H complex64 (P,K), X float32 (K,S)
 cudaError_t launch_weighted_tc(const void *H, const float *X, int64_t P, int64_t K, int64_t S, void *W, void *ws,
                                cudaStream_t st);
+// Float64 form on the tensor cores (bf16 digit slices, exact float32
+// accumulation; k_contract_tc.cu): out(K,S) complex128 += H^T E with H
+// complex128 (P,K), E float64 (P,S); ws holds oz_workspace_bytes(2K, S, P).
+// flag: device int, zero before the call; raised when H or E holds a
+// non-finite value, in which case these kernels leave out untouched and
+// launch_contract_f64_if computes the contraction.
+size_t oz_workspace_bytes(int64_t M, int64_t N, int64_t Kd);
+cudaError_t launch_contract_oz_expect(const void *H, const double *E, int64_t P, int64_t K, int64_t S, void *out,
+                                      void *ws, int *flag, cudaStream_t st);
+// The float64 CUDA-core contraction (complex128 H and out), run only when
+// *only_if != 0.
+cudaError_t launch_contract_f64_if(const void *H, const double *E, int64_t P, int64_t K, int64_t S, void *out,
+                                   const int *only_if, cudaStream_t st);
 // Reads and clears the tensor-core kernels' device error flag (synchronises st).
 cudaError_t read_device_error(int *code, cudaStream_t st);
 

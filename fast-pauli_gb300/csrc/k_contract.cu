@@ -11,7 +11,6 @@
 // Float64 arithmetic (the plain form).  64x64 output tiles, 16-deep k steps
 // staged in shared memory, 4x4 outputs per thread.
 #include "common.cuh"
-#include "df64.cuh"
 
 namespace fpg
 {
@@ -40,7 +39,7 @@ template <> struct HT<float2>
 // C(M,N) (+)= A(M,Kd) B(Kd,N); A complex, B real, C complex.
 // A_T: A(m,p) stored as Hs[p * lda + m] (transposed), else Hs[m * lda + p].
 // only_if: when not null, return at once unless *only_if is set (the float64
-// form after a df64 range check).
+// form behind the tensor-core contraction, for non-finite inputs).
 template <typename HC, typename BR, typename OC, bool A_T, bool ACCUM>
 __global__ void __launch_bounds__(256)
     k_gemm_cr(const void *__restrict__ Araw, int64_t lda, const BR *__restrict__ B, int64_t M, int64_t N, int64_t Kd,
@@ -142,155 +141,15 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// float64 value at p as df64 (hi, lo)
-__device__ __forceinline__ float2 ld_df(const double *p)
-{
-    const uint2 v = __ldg(reinterpret_cast<const uint2 *>(p));
-    float h, l;
-    split_bits(v.x, v.y, h, l);
-    return make_float2(h, l);
-}
-
-// The float64 contraction C(M,N) += A^T B (A: complex (Kd, M) = H, B: real
-// (Kd, N) = E, C complex) on the float32 pipes: operands split into df64
-// pairs when staged in shared memory, every product formed exactly
-// (df_fma) and every sum with TwoSum, so each output keeps ~2^-46 relative
-// accuracy of sum |terms| -- the float64 contraction at ~4x the speed of
-// GB300's float64 pipe.  Tiles as k_gemm_cr.
-// Returns at once when *skip_if is set (a value of H or E outside the df64
-// range: the float64 GEMM runs instead).
-__global__ void __launch_bounds__(256)
-    k_gemm_cr_df(const double *__restrict__ A, int64_t lda, const double *__restrict__ B, int64_t M, int64_t N,
-                 int64_t Kd, double2 *__restrict__ C, const int *__restrict__ skip_if)
-{
-    if (*skip_if)
-        return;
-    __shared__ float2 As_r[BK][BM];
-    __shared__ float2 As_i[BK][BM];
-    __shared__ float2 Bs[BK][BN];
-    const int tid = threadIdx.x;
-    const int tx = tid & 15, ty = tid >> 4;
-    const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
-    float cr[4][4][2], ci[4][4][2];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-            cr[i][j][0] = cr[i][j][1] = ci[i][j][0] = ci[i][j][1] = 0.f;
-
-    for (int64_t p0 = 0; p0 < Kd; p0 += BK)
-    {
-        for (int e = tid; e < BK * BM; e += 256)
-        {
-            const int kk = e / BM, mm = e % BM;
-            const int64_t p = p0 + kk, m = m0 + mm;
-            float2 ar = make_float2(0.f, 0.f), ai = ar;
-            if (p < Kd && m < M)
-            {
-                const double *src = A + 2 * (p * lda + m);
-                ar = ld_df(src);
-                ai = ld_df(src + 1);
-            }
-            As_r[kk][mm] = ar;
-            As_i[kk][mm] = ai;
-        }
-        for (int e = tid; e < BK * BN; e += 256)
-        {
-            const int kk = e / BN, nn = e % BN;
-            const int64_t p = p0 + kk, c = n0 + nn;
-            Bs[kk][nn] = (p < Kd && c < N) ? ld_df(B + p * N + c) : make_float2(0.f, 0.f);
-        }
-        __syncthreads();
-#pragma unroll 4
-        for (int kk = 0; kk < BK; ++kk)
-        {
-            float2 ar[4], ai[4], b[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-            {
-                ar[i] = As_r[kk][ty + 16 * i];
-                ai[i] = As_i[kk][ty + 16 * i];
-            }
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-                b[j] = Bs[kk][tx + 16 * j];
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 4; ++j)
-                {
-                    df_fma(ar[i].x, ar[i].y, b[j].x, b[j].y, cr[i][j][0], cr[i][j][1]);
-                    df_fma(ai[i].x, ai[i].y, b[j].x, b[j].y, ci[i][j][0], ci[i][j][1]);
-                }
-        }
-        // renormalise the accumulators once per k step (BK terms)
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-            {
-                df_norm(cr[i][j][0], cr[i][j][1]);
-                df_norm(ci[i][j][0], ci[i][j][1]);
-            }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-    {
-        const int64_t m = m0 + ty + 16 * i;
-        if (m >= M)
-            continue;
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-        {
-            const int64_t c = n0 + tx + 16 * j;
-            if (c >= N)
-                continue;
-            double2 &dst = C[m * N + c];
-            dst.x += df_to_double(cr[i][j][0], cr[i][j][1]);
-            dst.y += df_to_double(ci[i][j][0], ci[i][j][1]);
-        }
-    }
-}
-
-// *flag |= some float64 of a[0 .. na) or b[0 .. nb) lies outside the df64 range
-__global__ void k_df_range(const uint2 *__restrict__ a, int64_t na, const uint2 *__restrict__ b, int64_t nb,
-                           int *__restrict__ flag)
-{
-    bool bad = false;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < na + nb; i += (int64_t)gridDim.x * blockDim.x)
-        bad |= df_out_of_range(i < na ? __ldg(a + i).y : __ldg(b + (i - na)).y);
-    if (__syncthreads_or(bad) && threadIdx.x == 0)
-        atomicOr(flag, 1);
-}
-
 } // namespace
 
 cudaError_t launch_contract_real(bool out_c64, const void *H, bool h_c64, const double *E, int64_t P, int64_t K,
-                                 int64_t S, void *out, int *range_flag, cudaStream_t st)
+                                 int64_t S, void *out, cudaStream_t st)
 {
     if (K <= 0 || S <= 0)
         return cudaSuccess;
     dim3 grid((unsigned)((S + BN - 1) / BN), (unsigned)((K + BM - 1) / BM));
-    if (!out_c64 && !h_c64 && range_flag)
-    {
-        // float64: range check of H and E, then the df64 GEMM, or the float64
-        // GEMM when some value lies outside the df64 range (one of the two
-        // returns at once)
-        const int64_t nh = 2 * P * K, ne = P * S;
-        int64_t blocks = (nh + ne + 255) / 256;
-        if (blocks > 152 * 8)
-            blocks = 152 * 8;
-        k_df_range<<<(unsigned)blocks, 256, 0, st>>>((const uint2 *)H, nh, (const uint2 *)E, ne, range_flag);
-        if (cudaError_t e = launched())
-            return e;
-        k_gemm_cr_df<<<grid, 256, 0, st>>>((const double *)H, K, E, K, S, P, (double2 *)out, range_flag);
-        if (cudaError_t e = launched())
-            return e;
-        k_gemm_cr<double2, double, double2, true, true>
-            <<<grid, 256, 0, st>>>(H, K, E, K, S, P, (double2 *)out, range_flag);
-    }
-    else if (!out_c64 && !h_c64)
+    if (!out_c64 && !h_c64)
         k_gemm_cr<double2, double, double2, true, true><<<grid, 256, 0, st>>>(H, K, E, K, S, P, (double2 *)out, nullptr);
     else if (out_c64 && h_c64)
         k_gemm_cr<float2, double, float2, true, true><<<grid, 256, 0, st>>>(H, K, E, K, S, P, (float2 *)out, nullptr);
@@ -298,6 +157,17 @@ cudaError_t launch_contract_real(bool out_c64, const void *H, bool h_c64, const 
         k_gemm_cr<double2, double, float2, true, true><<<grid, 256, 0, st>>>(H, K, E, K, S, P, (float2 *)out, nullptr);
     else
         k_gemm_cr<float2, double, double2, true, true><<<grid, 256, 0, st>>>(H, K, E, K, S, P, (double2 *)out, nullptr);
+    return launched();
+}
+
+cudaError_t launch_contract_f64_if(const void *H, const double *E, int64_t P, int64_t K, int64_t S, void *out,
+                                   const int *only_if, cudaStream_t st)
+{
+    if (K <= 0 || S <= 0)
+        return cudaSuccess;
+    dim3 grid((unsigned)((S + BN - 1) / BN), (unsigned)((K + BM - 1) / BM));
+    k_gemm_cr<double2, double, double2, true, true>
+        <<<grid, 256, 0, st>>>(H, K, E, K, S, P, (double2 *)out, only_if);
     return launched();
 }
 

@@ -44,7 +44,7 @@ constexpr int TM = 128, TN = 128, TK = 32;           // CTA tile and k chunk (tf
 constexpr int BLOCK_BYTES = TM * TK * 4;             // 16 KiB per operand block
 constexpr int STAGE_BYTES = 4 * BLOCK_BYTES;         // A_hi, A_lo, B_hi, B_lo
 constexpr int NSTAGE = 2;
-constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024; // + barriers / TMEM address (alignment slack)
+constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 2048; // + 1024-byte alignment pad, barriers, TMEM address
 constexpr uint32_t TMEM_COLS = 128;
 constexpr long long WAIT_LIMIT = 1ll << 22;          // mbarrier polls before giving up
 
@@ -483,6 +483,504 @@ cudaError_t launch_weighted_tc(const void *H, const float *X, int64_t P, int64_t
     if ((e = run_gemm(g, st)))
         return e;
     k_finish_weighted<<<grid_for(P * S), 256, 0, st>>>(g.C, g.nseg, g.Mp * g.Np, g.Np, P, S, (float2 *)W);
+    return launched();
+}
+
+// ============================================================================
+// Float64 contraction on the tensor cores: digit slices with exact float32
+// accumulation (the Ozaki scheme).
+//
+// Published method: K. Ozaki, T. Ogita, S. Oishi, S. M. Rump, "Error-free
+// transformations of matrix multiplication by using fast routines of matrix
+// multiplication and its applications", Numer. Algorithms 59 (2012): split
+// both operands into slices whose pairwise products are computed without
+// rounding by a low-precision matrix engine, then add the slice products in
+// high precision.
+//
+// Here C(M,N) = A(M,Kd) B(N,Kd)^T with A = [Re H^T; Im H^T] (2K x P) and
+// B = E^T (S x P), the float64 contraction of SummedPauliOp::
+// expectation_value (fast_pauli/cpp/include/__summed_pauli_op.hpp:579-591).
+//  * Row scales: row r of A (and of B) gets 2^e_r > max_k |row r|; its element
+//    v becomes the integer V = rint(v 2^(55 - e_r)), |V| <= 2^55, an error of
+//    at most 2^-56 of the row maximum.
+//  * Digits: V = sum_{s=1..8} d_s 128^(8-s) with d_2..d_8 in [-64, 63] and
+//    |d_1| <= 65 -- every digit is exact in bf16, every digit product is an
+//    integer below 65^2 < 2^12.1.
+//  * Levels: the pairs (s, r) with s + r = L have equal weight 128^(16-L) and
+//    share a float32 accumulator in TMEM; levels 2..9 are kept (36 of the 64
+//    pairs; a term of the first dropped level is below 2^-55 of
+//    rowmax * colmax).  A level holds at most 8 pairs, so over a 448-deep k
+//    segment its sum stays below 8 * 448 * 65^2 < 2^24 and is exact: the
+//    tensor core's float32 accumulation rounds nothing.
+//  * Epilogue: per segment, the eight exact level sums of an output are
+//    folded into a double-float value (TwoSum); the finishing kernel sums the
+//    segments in float64 and applies 2^(e_row + e_col - 12).
+// Modelled in numpy on config-2-like data (P = 861, Gaussian H, expectation
+// columns with 30x outliers): 1.4e-15 normwise against the float64 GEMM
+// (seven digits and levels up to 8: 1.6e-13).  A non-finite value
+// in H or E raises the call's flag instead; the float64 CUDA-core GEMM then
+// computes the contraction (every kernel here returns at once).
+namespace
+{
+
+constexpr int OZ_SLICES = 8;                  // digits per element
+constexpr int OZ_LMAX = 9;                    // levels 2..OZ_LMAX kept
+constexpr int OZ_LEVELS = OZ_LMAX - 1;
+constexpr int OZ_TM = 128, OZ_TN = 64, OZ_TK = 16;       // CTA tile, k chunk (bf16 elements)
+constexpr int OZ_SBO = 8 * OZ_TK * 2;                    // bytes between 8-row core-matrix groups
+constexpr int OZ_A_BLOCK = OZ_TM * OZ_TK * 2;            // 4 KiB
+constexpr int OZ_B_BLOCK = OZ_TN * OZ_TK * 2;            // 2 KiB
+constexpr int OZ_STAGE = OZ_SLICES * (OZ_A_BLOCK + OZ_B_BLOCK);
+constexpr int OZ_NSTAGE = 4;
+constexpr int OZ_SMEM = OZ_NSTAGE * OZ_STAGE + 2048; // + 1024-byte alignment pad, barriers
+constexpr uint32_t OZ_TMEM_COLS = 512;                   // OZ_LEVELS x OZ_TN
+constexpr int64_t OZ_SEG_CHUNKS = 448 / OZ_TK;           // 448-deep exact segments
+static_assert((OZ_LMAX - 1) * OZ_SEG_CHUNKS * OZ_TK * 65 * 65 < (1 << 24), "level sums must stay exact");
+static_assert(OZ_LEVELS * OZ_TN <= (int)OZ_TMEM_COLS, "levels must fit in TMEM");
+static_assert(OZ_SMEM <= 227 * 1024, "stage ring must fit in shared memory");
+
+// kind::f16: D = f32 (bits 4-5 = 1), A = B = bf16 (bits 7-9 and 10-12 = 1),
+// both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t OZ_IDESC =
+    (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_TN >> 3) << 17) | ((uint32_t)(OZ_TM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t accumulate)
+{
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "setp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+                 "l"(da), "l"(db), "r"(OZ_IDESC), "r"(accumulate));
+}
+
+// 2^e as a float (-126 <= e <= 127), from its bits
+__device__ __forceinline__ float pow2f(int e)
+{
+    return __uint_as_float((uint32_t)(127 + e) << 23);
+}
+
+// byte offset of element (r, k) inside an R x OZ_TK bf16 block
+__device__ __forceinline__ uint32_t oz_offset(int r, int k)
+{
+    return (uint32_t)((r >> 3) * OZ_SBO + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// exponent e with |x| < 2^e for every x of a row whose maximum has these bits
+// (0 for an all-zero row, whose digits are all zero)
+__device__ __forceinline__ int oz_exponent(unsigned long long maxbits)
+{
+    const double mx = __longlong_as_double((long long)maxbits);
+    int e = 0;
+    if (mx > 0.0)
+        (void)frexp(mx, &e);
+    return e;
+}
+
+// Row maxima of A = [Re H^T; Im H^T]: maxbits[m] (m < K: real parts of column
+// m of H; K + m: imaginary parts), as bit patterns (non-negative doubles
+// order like their bits).  *bad |= a non-finite value.
+__global__ void k_oz_max_h(const double2 *__restrict__ H, int64_t P, int64_t K, int64_t rows_per_block,
+                           unsigned long long *__restrict__ maxbits, int *__restrict__ bad)
+{
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= K)
+        return;
+    const int64_t p0 = (int64_t)blockIdx.y * rows_per_block, p1 = min(P, p0 + rows_per_block);
+    double mr = 0.0, mi = 0.0;
+    bool nf = false;
+    for (int64_t p = p0; p < p1; ++p)
+    {
+        const double2 h = H[p * K + k];
+        nf |= !isfinite(h.x) || !isfinite(h.y);
+        mr = fmax(mr, fabs(h.x));
+        mi = fmax(mi, fabs(h.y));
+    }
+    if (nf)
+        atomicOr(bad, 1);
+    atomicMax(&maxbits[k], (unsigned long long)__double_as_longlong(mr));
+    atomicMax(&maxbits[K + k], (unsigned long long)__double_as_longlong(mi));
+}
+
+// Row maxima of B = E^T: maxbits[t] = max_p |E[p][t]|.
+__global__ void k_oz_max_e(const double *__restrict__ E, int64_t P, int64_t S, int64_t rows_per_block,
+                           unsigned long long *__restrict__ maxbits, int *__restrict__ bad)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= S)
+        return;
+    const int64_t p0 = (int64_t)blockIdx.y * rows_per_block, p1 = min(P, p0 + rows_per_block);
+    double m = 0.0;
+    bool nf = false;
+    for (int64_t p = p0; p < p1; ++p)
+    {
+        const double v = E[p * S + t];
+        nf |= !isfinite(v);
+        m = fmax(m, fabs(v));
+    }
+    if (nf)
+        atomicOr(bad, 1);
+    atomicMax(&maxbits[t], (unsigned long long)__double_as_longlong(m));
+}
+
+// The seven digit slices of an operand, each in OZ_TK-deep blocks of
+// tile_rows rows in the canonical K-major core-matrix layout:
+// block (s, row tile, k chunk) at ((s * tiles + tile) * kchunks + chunk).
+// One thread per (row, 8-deep k group) writes 16 bytes per slice.
+// A operand (IS_H): element (m, p) = m < K ? Re H[p][m] : Im H[p][m-K];
+// B operand: element (t, p) = E[p][t].
+template <bool IS_H>
+__global__ void k_oz_slice(const void *__restrict__ src, int64_t P, int64_t width, int64_t rows, int64_t rows_pad,
+                           int64_t depth_pad, int tile_rows, const unsigned long long *__restrict__ maxbits,
+                           const int *__restrict__ skip_if, unsigned char *__restrict__ slices)
+{
+    if (*skip_if)
+        return;
+    const int64_t kgroups = depth_pad / 8, kchunks = depth_pad / OZ_TK, tiles = rows_pad / tile_rows;
+    const int64_t block_bytes = (int64_t)tile_rows * OZ_TK * 2;
+    const int64_t total = rows_pad * kgroups;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int64_t r = e % rows_pad, kg = e / rows_pad;
+        const int ex = r < rows ? oz_exponent(maxbits[r]) : 0;
+        uint32_t packed[OZ_SLICES][4];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+        {
+            const int64_t k = kg * 8 + j;
+            double v = 0.0;
+            if (r < rows && k < P)
+            {
+                if constexpr (IS_H)
+                {
+                    const double2 *H = (const double2 *)src;
+                    v = r < width ? H[k * width + r].x : H[k * width + (r - width)].y;
+                }
+                else
+                {
+                    v = ((const double *)src)[k * width + r];
+                }
+            }
+            long long n = llrint(ldexp(v, 55 - ex)); // |n| <= 2^55
+            int d[OZ_SLICES];
+#pragma unroll
+            for (int s = OZ_SLICES - 1; s >= 1; --s)
+            {
+                d[s] = (int)((n + 64) & 127) - 64; // balanced digit in [-64, 63]
+                n = (n - d[s]) >> 7;               // exact: n - d[s] is a multiple of 128
+            }
+            d[0] = (int)n; // |d_1| <= 2^55 / 128^7 + 1/2 -> <= 65
+#pragma unroll
+            for (int s = 0; s < OZ_SLICES; ++s)
+            {
+                // an integer of magnitude <= 256 is exact in bf16: its bits are
+                // the top half of the float's
+                const uint32_t b = __float_as_uint((float)d[s]) >> 16;
+                if (j & 1)
+                    packed[s][j >> 1] |= b << 16;
+                else
+                    packed[s][j >> 1] = b;
+            }
+        }
+        const int64_t tile = r / tile_rows, chunk = kg / (OZ_TK / 8);
+        const uint32_t off = oz_offset((int)(r % tile_rows), (int)(kg % (OZ_TK / 8)) * 8);
+#pragma unroll
+        for (int s = 0; s < OZ_SLICES; ++s)
+        {
+            unsigned char *dst = slices + ((s * tiles + tile) * kchunks + chunk) * block_bytes + off;
+            *reinterpret_cast<uint4 *>(dst) = make_uint4(packed[s][0], packed[s][1], packed[s][2], packed[s][3]);
+        }
+    }
+}
+
+// One 128 x 64 tile of one 448-deep k segment per CTA (blockIdx.z =
+// segment): the level sums accumulate in TMEM (level L at columns
+// (L-2) * 64), and the epilogue writes each output's folded double-float
+// value (hi, lo) of the segment to C[z] (rows_pad x cols_pad float2).
+__global__ void __launch_bounds__(128, 1)
+    k_gemm_oz(const unsigned char *__restrict__ a_sl, const unsigned char *__restrict__ b_sl, int64_t kchunks,
+              int64_t mtiles, int64_t ntiles, int64_t rows_pad, int64_t cols_pad, float2 *__restrict__ C,
+              const int *__restrict__ skip_if)
+{
+    if (*skip_if)
+        return;
+    const int64_t kb = (int64_t)blockIdx.z * OZ_SEG_CHUNKS;
+    const int64_t nk = min(kchunks, kb + OZ_SEG_CHUNKS) - kb; // chunks of this segment (>= 1)
+    C += (int64_t)blockIdx.z * rows_pad * cols_pad;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *full = (uint64_t *)(smem + OZ_NSTAGE * OZ_STAGE);
+    uint64_t *empty = full + OZ_NSTAGE;
+    uint64_t *done = empty + OZ_NSTAGE;
+    uint32_t *tmem_slot = (uint32_t *)(done + 1);
+    int *status = (int *)(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t mt = blockIdx.y, nt = blockIdx.x;
+
+    if (threadIdx.x == 0)
+    {
+        for (int s = 0; s < OZ_NSTAGE; ++s)
+        {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        *status = 1;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(OZ_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (threadIdx.x == 0)
+    {
+        bool ok = true;
+        auto issue = [&](int64_t kc, int s) {
+            unsigned char *stage = smem + s * OZ_STAGE;
+            mbar_expect_tx(&full[s], OZ_STAGE);
+            for (int q = 0; q < OZ_SLICES; ++q)
+                bulk_copy_g2s(stage + q * OZ_A_BLOCK, a_sl + ((q * mtiles + mt) * kchunks + kb + kc) * OZ_A_BLOCK,
+                              OZ_A_BLOCK, &full[s]);
+            for (int q = 0; q < OZ_SLICES; ++q)
+                bulk_copy_g2s(stage + OZ_SLICES * OZ_A_BLOCK + q * OZ_B_BLOCK,
+                              b_sl + ((q * ntiles + nt) * kchunks + kb + kc) * OZ_B_BLOCK, OZ_B_BLOCK, &full[s]);
+        };
+        uint32_t full_phase[OZ_NSTAGE], empty_phase[OZ_NSTAGE];
+        bool pending[OZ_NSTAGE];
+        for (int s = 0; s < OZ_NSTAGE; ++s)
+        {
+            full_phase[s] = empty_phase[s] = 0;
+            pending[s] = false;
+        }
+        int64_t issued = 0;
+        for (; issued < nk && issued < OZ_NSTAGE; ++issued)
+        {
+            issue(issued, (int)issued);
+            pending[issued] = true;
+        }
+        for (int64_t kc = 0; kc < nk; ++kc)
+        {
+            const int s = (int)(kc % OZ_NSTAGE);
+            if (!mbar_wait(&full[s], full_phase[s]))
+            {
+                ok = false;
+                break;
+            }
+            full_phase[s] ^= 1u;
+            pending[s] = false;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t base = smem_u32(smem + s * OZ_STAGE);
+#pragma unroll
+            for (int L = 2; L <= OZ_LMAX; ++L)
+            {
+                const int s_lo = L - OZ_SLICES > 1 ? L - OZ_SLICES : 1;
+                const int s_hi = L - 1 < OZ_SLICES ? L - 1 : OZ_SLICES;
+                for (int sa = s_lo; sa <= s_hi; ++sa)
+                {
+                    const int sb = L - sa;
+                    const uint64_t da = smem_desc(base + (uint32_t)((sa - 1) * OZ_A_BLOCK), 128, OZ_SBO);
+                    const uint64_t db =
+                        smem_desc(base + (uint32_t)(OZ_SLICES * OZ_A_BLOCK + (sb - 1) * OZ_B_BLOCK), 128, OZ_SBO);
+                    const uint32_t acc = (kc > 0 || sa > s_lo) ? 1u : 0u;
+                    mma_bf16(tmem + (uint32_t)((L - 2) * OZ_TN), da, db, acc);
+                }
+            }
+            mma_commit(&empty[s]);
+            // refill the stage of the previous chunk, whose MMAs were issued
+            // one chunk earlier (one chunk of MMAs stays queued meanwhile)
+            if (kc >= 1 && issued < nk)
+            {
+                const int sp = (int)((kc - 1) % OZ_NSTAGE);
+                if (!mbar_wait(&empty[sp], empty_phase[sp]))
+                {
+                    ok = false;
+                    break;
+                }
+                empty_phase[sp] ^= 1u;
+                issue(issued, sp);
+                pending[sp] = true;
+                ++issued;
+            }
+        }
+        mma_commit(done);
+        if (!ok)
+        {
+            atomicExch(&g_tc_error, 1);
+            // drain our own copies still in flight (bounded)
+            for (int s = 0; s < OZ_NSTAGE; ++s)
+                if (pending[s])
+                    (void)mbar_wait(&full[s], full_phase[s]);
+        }
+        *status = ok ? 1 : 0;
+    }
+    __syncthreads();
+    const bool ok = *status != 0;
+    const bool done_ok = mbar_wait(done, 0);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+    if (done_ok && ok)
+    {
+        const int64_t row = mt * OZ_TM + warp * 32 + lane;
+        float2 *dst_row = C + row * cols_pad + nt * OZ_TN;
+        for (int c0 = 0; c0 < OZ_TN; c0 += 8)
+        {
+            uint32_t v[OZ_LEVELS][8];
+#pragma unroll
+            for (int l = 0; l < OZ_LEVELS; ++l)
+            {
+                const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(l * OZ_TN + c0);
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                             : "=r"(v[l][0]), "=r"(v[l][1]), "=r"(v[l][2]), "=r"(v[l][3]), "=r"(v[l][4]),
+                               "=r"(v[l][5]), "=r"(v[l][6]), "=r"(v[l][7])
+                             : "r"(taddr));
+            }
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            float2 out[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+            {
+                // level L (index l = L - 2) weighs 128^(-l) relative to level 2;
+                // add from the smallest weight up, exactly (TwoSum)
+                float hi = __fmul_rn(__uint_as_float(v[OZ_LEVELS - 1][j]), pow2f(-7 * (OZ_LEVELS - 1)));
+                float lo = 0.0f;
+#pragma unroll
+                for (int l = OZ_LEVELS - 2; l >= 0; --l)
+                {
+                    const float t = __fmul_rn(__uint_as_float(v[l][j]), pow2f(-7 * l));
+                    const float s = __fadd_rn(hi, t);
+                    const float bb = __fsub_rn(s, hi);
+                    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(t, bb));
+                    hi = s;
+                    lo = __fadd_rn(lo, err);
+                }
+                const float s = __fadd_rn(hi, lo);
+                out[j] = make_float2(s, __fsub_rn(lo, __fsub_rn(s, hi)));
+            }
+#pragma unroll
+            for (int j = 0; j < 8; j += 2)
+                *reinterpret_cast<float4 *>(dst_row + c0 + j) = make_float4(out[j].x, out[j].y, out[j + 1].x,
+                                                                            out[j + 1].y);
+        }
+    }
+    else if (threadIdx.x == 0)
+    {
+        atomicExch(&g_tc_error, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(OZ_TMEM_COLS)
+                     : "memory");
+}
+
+// out[k][t] += (sum_z C[z][k][t], sum_z C[z][K+k][t]) * 2^(e_row + e_col - 12)
+__global__ void k_oz_finish(const float2 *__restrict__ C, int64_t nseg, int64_t seg_stride, int64_t cols_pad,
+                            int64_t K, int64_t S, const unsigned long long *__restrict__ max_a,
+                            const unsigned long long *__restrict__ max_b, const int *__restrict__ skip_if,
+                            double2 *__restrict__ out)
+{
+    if (*skip_if)
+        return;
+    const int64_t total = K * S;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int64_t k = e / S, t = e - k * S;
+        const int eb = oz_exponent(max_b[t]);
+        double re = 0.0, im = 0.0;
+        for (int64_t z = 0; z < nseg; ++z)
+        {
+            const float2 a = C[z * seg_stride + k * cols_pad + t];
+            const float2 b = C[z * seg_stride + (K + k) * cols_pad + t];
+            re += (double)a.x + (double)a.y;
+            im += (double)b.x + (double)b.y;
+        }
+        double2 o = out[e];
+        o.x += ldexp(re, oz_exponent(max_a[k]) + eb - 12);
+        o.y += ldexp(im, oz_exponent(max_a[K + k]) + eb - 12);
+        out[e] = o;
+    }
+}
+
+struct OzLayout
+{
+    int64_t Mp, Np, Kp, kchunks, nseg;
+    unsigned long long *max_a, *max_b;
+    unsigned char *a_sl, *b_sl;
+    float2 *C;
+};
+
+OzLayout oz_layout(int64_t M, int64_t N, int64_t Kd, void *ws)
+{
+    OzLayout g{};
+    g.Mp = round_up(M, OZ_TM);
+    g.Np = round_up(N, OZ_TN);
+    g.Kp = round_up(Kd, OZ_TK);
+    g.kchunks = g.Kp / OZ_TK;
+    g.nseg = (g.kchunks + OZ_SEG_CHUNKS - 1) / OZ_SEG_CHUNKS;
+    unsigned char *p = (unsigned char *)(((uintptr_t)ws + 255) & ~(uintptr_t)255);
+    g.max_a = (unsigned long long *)p;
+    g.max_b = g.max_a + g.Mp;
+    p += round_up((g.Mp + g.Np) * 8, 256);
+    g.a_sl = p;
+    p += OZ_SLICES * g.Mp * g.Kp * 2;
+    g.b_sl = p;
+    p += OZ_SLICES * g.Np * g.Kp * 2;
+    g.C = (float2 *)p;
+    return g;
+}
+
+} // namespace
+
+size_t oz_workspace_bytes(int64_t M, int64_t N, int64_t Kd)
+{
+    const OzLayout g = oz_layout(M, N, Kd, nullptr);
+    return (size_t)(round_up((g.Mp + g.Np) * 8, 256) + OZ_SLICES * (g.Mp + g.Np) * g.Kp * 2 +
+                    g.nseg * g.Mp * g.Np * 8) +
+           256;
+}
+
+cudaError_t launch_contract_oz_expect(const void *H, const double *E, int64_t P, int64_t K, int64_t S, void *out,
+                                      void *ws, int *flag, cudaStream_t st)
+{
+    if (K <= 0 || S <= 0 || P <= 0)
+        return cudaSuccess;
+    const OzLayout g = oz_layout(2 * K, S, P, ws);
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(g.max_a, 0, (size_t)(g.Mp + g.Np) * 8, st)))
+        return e;
+    const int64_t rows_per_block = P > 32 * 4096 ? (P + 4095) / 4096 : 32; // grid y <= 4096
+    const unsigned py = (unsigned)((P + rows_per_block - 1) / rows_per_block);
+    k_oz_max_h<<<dim3((unsigned)((K + 127) / 128), py), 128, 0, st>>>((const double2 *)H, P, K, rows_per_block,
+                                                                      g.max_a, flag);
+    if ((e = launched()))
+        return e;
+    k_oz_max_e<<<dim3((unsigned)((S + 127) / 128), py), 128, 0, st>>>(E, P, S, rows_per_block, g.max_b, flag);
+    if ((e = launched()))
+        return e;
+    k_oz_slice<true><<<grid_for(g.Mp * (g.Kp / 8)), 256, 0, st>>>(H, P, K, 2 * K, g.Mp, g.Kp, OZ_TM, g.max_a, flag,
+                                                                  g.a_sl);
+    if ((e = launched()))
+        return e;
+    k_oz_slice<false><<<grid_for(g.Np * (g.Kp / 8)), 256, 0, st>>>(E, P, S, S, g.Np, g.Kp, OZ_TN, g.max_b, flag,
+                                                                   g.b_sl);
+    if ((e = launched()))
+        return e;
+    if ((e = cudaFuncSetAttribute(k_gemm_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM)))
+        return e;
+    dim3 grid((unsigned)(g.Np / OZ_TN), (unsigned)(g.Mp / OZ_TM), (unsigned)g.nseg);
+    k_gemm_oz<<<grid, 128, OZ_SMEM, st>>>(g.a_sl, g.b_sl, g.kchunks, g.Mp / OZ_TM, g.Np / OZ_TN, g.Mp, g.Np, g.C,
+                                          flag);
+    if ((e = launched()))
+        return e;
+    k_oz_finish<<<grid_for(K * S), 256, 0, st>>>(g.C, g.nseg, g.Mp * g.Np, g.Np, K, S, g.max_a, g.max_b, flag,
+                                                 (double2 *)out);
     return launched();
 }
 

@@ -242,7 +242,7 @@ extern "C" int fpg_summed_expect_noalloc(const char *strings, int64_t n_strings,
         if (en > b && (e = launch_expect_chunks(fp32, states, S, n_qubits, dop, d_chunks + b, en - b, c, plan, ev, st)))
             return cuda_error(e, "expectation kernel");
     }
-    if ((e = launch_contract_real(fp32, coeffs, fp32, ev, P, n_operators, S, out, nullptr, st)))
+    if ((e = launch_contract_real(fp32, coeffs, fp32, ev, P, n_operators, S, out, st)))
         return cuda_error(e, "contraction kernel");
     return FPG_OK;
 }

@@ -238,6 +238,51 @@ def test_float64_path_far_from_unit_scale(scale_psi, scale_h):
     assert normwise(got, want) < TOL_C128
 
 
+def test_float64_contraction_mixed_magnitudes():
+    """The float64 contraction scales every row of H^T and of the per-string
+    expectation table by a power of two and multiplies digit slices on the
+    tensor cores: coefficients spanning 16 decades inside one operator, an
+    all-zero operator and 300 columns (a ragged 64-column tile) must still
+    meet the float64 tolerance."""
+    rng = np.random.default_rng(62)
+    n, S, K = 8, 300, 7
+    strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
+    P = len(strings)
+    mag = 10.0 ** rng.uniform(-8, 8, size=(P, K))
+    h = (rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))) * mag
+    h[:, 3] = 0
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    want = oracle.summed_expectation(strings, h, psi)
+    got = fp.SummedPauliOp(strings, h).expectation_value(psi)
+    assert normwise(got, want) < TOL_C128
+    assert np.all(got[3] == 0)
+    for k in (0, 1, 2, 4, 5, 6):
+        assert normwise(got[k], want[k]) < TOL_C128
+
+
+def test_float64_contraction_non_finite_coefficients():
+    """A non-finite coefficient routes the contraction to the float64 GEMM:
+    infinities and NaNs land where plain float64 arithmetic puts them."""
+    rng = np.random.default_rng(63)
+    n, S, K = 6, 9, 4
+    strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
+    P = len(strings)
+    h = rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))
+    h[2, 1] = np.inf
+    h[5, 3] = complex(np.nan, 0.0)
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    ev = np.stack([oracle.string_expectation(s, psi).real for s in strings])  # (P, S)
+    # real and imaginary parts contract separately (E is real)
+    with np.errstate(invalid="ignore"):
+        want = h.real.T @ ev + 1j * (h.imag.T @ ev)
+    got = fp.SummedPauliOp(strings, h).expectation_value(psi)
+    np.testing.assert_array_equal(np.isnan(got.real), np.isnan(want.real))
+    np.testing.assert_array_equal(np.isinf(got.real), np.isinf(want.real))
+    np.testing.assert_array_equal(np.isnan(got.imag), np.isnan(want.imag))
+    fin = np.isfinite(want)
+    assert normwise(got[fin], want[fin]) < TOL_C128
+
+
 def test_exhaustive_small_strings_vs_dense():
     rng = np.random.default_rng(3)
     for n in (1, 2, 3):
