@@ -21,7 +21,7 @@
  *    __summed_pauli_op.hpp:609): callers zero them first.
  *  - Work is ordered on `stream` (a cudaStream_t, NULL = legacy default
  *    stream); functions return once the work is enqueued.  Scratch memory is
- *    drawn from the device's stream-ordered pool (cudaMallocAsync).
+ *    drawn from the library's stream-ordered pool (fpg_device_alloc).
  *  - dtype FPG_C128: complex128 data, float64 arithmetic (the reference's
  *    precision).  dtype FPG_C64: complex64 data, float32 arithmetic with
  *    compensated float32 partial sums, float64 cross-block reduction, 3xTF32

@@ -104,6 +104,32 @@ def test_weight2_strings_summed_expectation(n, S):
     assert normwise(got, oracle.summed_expectation(strings, h, psi)) < TOL_C128
 
 
+@pytest.mark.parametrize("kind", ["weight2", "uniform", "weight2_c64", "weight2_tiny"])
+def test_pinned_host_states(kind):
+    """Pinned host states (as torch's pinned tensors give them): float64 and
+    complex64, operators with and without direct chunks, amplitudes outside
+    the double-float range."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(91)
+    n, S, K = 9, 24, 3
+    if kind == "uniform":
+        strings = oracle.uniform_strings(rng, n, 30)
+    else:
+        strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
+    P = len(strings)
+    h = (rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))) / np.sqrt(2 * P)
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    if kind == "weight2_tiny":
+        psi *= 1e-30
+    want = oracle.summed_expectation(strings, h, psi)
+    dt = torch.complex64 if kind == "weight2_c64" else torch.complex128
+    t = torch.empty(psi.shape, dtype=dt, pin_memory=True)
+    t.copy_(torch.from_numpy(psi))
+    got = fp.SummedPauliOp(strings, h).expectation_value(t.numpy())
+    tol = TOL_MIXED if kind == "weight2_c64" else TOL_C128
+    assert normwise(got, want) < tol
+
+
 def test_pool_memory_reused_and_released():
     # temporaries come from the library's pool: back-to-back host-buffer
     # calls (each synchronises) reuse it; after release_cached_memory the
