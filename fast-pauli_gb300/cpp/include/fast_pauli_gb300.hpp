@@ -677,6 +677,20 @@ inline std::string join_strings(std::vector<PauliString> const &ps)
 }
 
 // Encoded-operator cache keyed by the strings' content.
+// PauliString of the (x, z) masks (bit n-1-q is character q)
+inline PauliString string_from_masks(uint64_t x, uint64_t z, size_t n)
+{
+    std::vector<Pauli> ps;
+    ps.reserve(n);
+    for (size_t q = 0; q < n; ++q)
+    {
+        const int b = (int)(n - 1 - q);
+        const bool xb = (x >> b) & 1ull, zb = (z >> b) & 1ull;
+        ps.push_back(Pauli(xb ? (zb ? 'Y' : 'X') : (zb ? 'Z' : 'I')));
+    }
+    return PauliString(std::move(ps));
+}
+
 class EncodedCache
 {
   public:
@@ -812,31 +826,61 @@ template <std::floating_point T, typename H = std::complex<T>> struct PauliOp
         }
         return PauliOp(std::move(c), std::move(s));
     }
-    // Product of two operators with duplicate strings merged (reference
-    // :237-281).  The result lists strings in order of first appearance.
+    // Product of two operators with equal strings merged (reference
+    // :237-281), on the GPU (fpg_op_product): the distinct product strings
+    // ordered by their (x, z) encoding, coefficients summed in pair order.
+    // (The reference's order is that of its per-thread hash maps.)
     friend PauliOp operator*(PauliOp const &lhs, PauliOp const &rhs)
     {
         if (lhs.dim() != rhs.dim())
             throw std::invalid_argument("Mismatched dimensions for provided PauliOp");
-        std::unordered_map<PauliString, size_t> where;
+        const size_t Pa = lhs.n_pauli_strings(), Pb = rhs.n_pauli_strings();
+        if (Pa == 0 || Pb == 0)
+            return PauliOp();
+        const size_t n = lhs.pauli_strings[0].n_qubits();
+        using CD = std::complex<double>;
+        if (n == 0)
+        {
+            // strings without characters: scalars
+            CD sa = 0, sb = 0;
+            for (auto const &c : lhs.coeffs)
+                sa += CD(c);
+            for (auto const &c : rhs.coeffs)
+                sb += CD(c);
+            return PauliOp(std::vector<H>{H(sa * sb)}, std::vector<PauliString>{PauliString(std::vector<Pauli>{})});
+        }
+        fpg_operator *oa = lhs.cache_.get(lhs.pauli_strings), *ob = rhs.cache_.get(rhs.pauli_strings);
+        cudaStream_t st = detail::stream();
+        const std::vector<CD> ca(lhs.coeffs.begin(), lhs.coeffs.end()), cb(rhs.coeffs.begin(), rhs.coeffs.end());
+        const size_t N = Pa * Pb;
+        detail::DevBuf da(Pa * sizeof(CD), st), db(Pb * sizeof(CD), st), ox(N * 8, st), oz(N * 8, st),
+            oc(N * sizeof(CD), st);
+        detail::cuda_check(cudaMemcpyAsync(da.p, ca.data(), da.bytes, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
+        detail::cuda_check(cudaMemcpyAsync(db.p, cb.data(), db.bytes, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
+        int64_t n_out = 0;
+        detail::check(fpg_op_product(oa, da.p, ob, db.p, (uint64_t *)ox.p, (uint64_t *)oz.p, oc.p, &n_out, st));
+        std::vector<uint64_t> hx((size_t)n_out), hz((size_t)n_out);
+        std::vector<CD> hc((size_t)n_out);
+        if (n_out > 0)
+        {
+            detail::cuda_check(cudaMemcpyAsync(hx.data(), ox.p, hx.size() * 8, cudaMemcpyDeviceToHost, st),
+                               "cudaMemcpyAsync");
+            detail::cuda_check(cudaMemcpyAsync(hz.data(), oz.p, hz.size() * 8, cudaMemcpyDeviceToHost, st),
+                               "cudaMemcpyAsync");
+            detail::cuda_check(cudaMemcpyAsync(hc.data(), oc.p, hc.size() * sizeof(CD), cudaMemcpyDeviceToHost, st),
+                               "cudaMemcpyAsync");
+        }
+        detail::sync(st);
         std::vector<H> c;
-        std::vector<PauliString> s;
-        for (size_t i = 0; i < lhs.n_pauli_strings(); ++i)
-            for (size_t j = 0; j < rhs.n_pauli_strings(); ++j)
-            {
-                auto [ph, p] = lhs.pauli_strings[i] * rhs.pauli_strings[j];
-                const H cij = H(ph) * lhs.coeffs[i] * rhs.coeffs[j];
-                auto it = where.find(p);
-                if (it == where.end())
-                {
-                    where.emplace(p, s.size());
-                    c.push_back(cij);
-                    s.push_back(std::move(p));
-                }
-                else
-                    c[it->second] += cij;
-            }
-        return PauliOp(std::move(c), std::move(s));
+        std::vector<PauliString> strs;
+        c.reserve(hc.size());
+        strs.reserve(hc.size());
+        for (size_t k = 0; k < hc.size(); ++k)
+        {
+            c.push_back(H(hc[k]));
+            strs.push_back(detail::string_from_masks(hx[k], hz[k], n));
+        }
+        return PauliOp(std::move(c), std::move(strs));
     }
 
     void extend(PauliString pauli_str, std::complex<T> coeff, bool dedupe = true)

@@ -1020,6 +1020,36 @@ extern "C"
         return FPG_OK;
     }
 
+    int fpg_op_product(const fpg_operator *a, const void *coeffs_a, const fpg_operator *b, const void *coeffs_b,
+                       uint64_t *out_x, uint64_t *out_z, void *out_coeffs, int64_t *n_out, void *stream)
+    {
+        if (!a || !b || !n_out)
+            return set_error(FPG_ERR_INVALID, "a, b and n_out must not be null");
+        *n_out = 0;
+        const int64_t Pa = a->P, Pb = b->P;
+        if (Pa == 0 || Pb == 0)
+            return FPG_OK;
+        if (a->n != b->n)
+            return set_error(FPG_ERR_INVALID, "Mismatched dimensions for provided PauliOp");
+        if (a->device != b->device)
+            return set_error(FPG_ERR_INVALID, "the operators live on different devices");
+        if (!coeffs_a || !coeffs_b || !out_x || !out_z || !out_coeffs)
+            return set_error(FPG_ERR_INVALID, "null array");
+        if (int rc = check_aligned(FPG_C128, {coeffs_a, coeffs_b, out_coeffs}))
+            return rc;
+        if (Pa * Pb >= ((int64_t)1 << 31))
+            return set_error(FPG_ERR_UNSUPPORTED, "too many string pairs (n_strings(a) * n_strings(b) >= 2^31)");
+        DeviceGuard g(a->device);
+        if (!g.ok)
+            return set_error(FPG_ERR_CUDA, "cannot select the operator's device");
+        cudaStream_t st = (cudaStream_t)stream;
+        Scratch ws(st);
+        FPG_CUDA(ws.alloc(product_workspace_bytes(Pa, Pb)));
+        FPG_CUDA(launch_op_product(a->dev(), coeffs_a, b->dev(), coeffs_b, a->n, ws.p, out_x, out_z, out_coeffs, n_out,
+                                   st));
+        return FPG_OK;
+    }
+
     int fpg_summed_square(const fpg_operator *op, const void *coeffs, int64_t n_operators, const fpg_operator *sq,
                           void *out, int32_t dtype, void *stream)
     {

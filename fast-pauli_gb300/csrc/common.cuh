@@ -276,6 +276,16 @@ size_t square_workspace_bytes(int64_t P, int64_t A);
 cudaError_t launch_square(bool fp32, const DevOp &op, const DevOp &sq, const void *h, int64_t K, void *out,
                           void *ws, unsigned long long **found, cudaStream_t st);
 
+// PauliOp product with equal strings merged (k_product.cu): the distinct
+// strings among the products of a's and b's strings as (x, z) masks sorted
+// by (x, z), and their complex128 coefficients; out arrays hold a.P * b.P
+// entries (< 2^31), *n_out (host) the count; ws holds
+// product_workspace_bytes(a.P, b.P).  Synchronises st.
+size_t product_workspace_bytes(int64_t Pa, int64_t Pb);
+cudaError_t launch_op_product(const DevOp &a, const void *coeffs_a, const DevOp &b, const void *coeffs_b, int n,
+                              void *ws, uint64_t *out_x, uint64_t *out_z, void *out_c, int64_t *n_out,
+                              cudaStream_t st);
+
 // out(k, i, j) += (sum_j coeffs(j,k) P_j)(i, j): the dense matrices of K
 // operators, out (K, 2^n, 2^n) complex.
 cudaError_t launch_to_tensor(bool fp32, const DevOp &op, const void *coeffs, int64_t K, void *out, cudaStream_t st);

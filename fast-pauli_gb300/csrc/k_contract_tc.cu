@@ -630,7 +630,7 @@ __global__ void k_oz_max_e(const double *__restrict__ E, int64_t P, int64_t S, i
 template <bool IS_H>
 __global__ void k_oz_slice(const void *__restrict__ src, int64_t P, int64_t width, int64_t rows, int64_t rows_pad,
                            int64_t depth_pad, int tile_rows, const unsigned long long *__restrict__ maxbits,
-                           const int *__restrict__ skip_if, unsigned char *__restrict__ slices)
+                           const int *__restrict__ skip_if, unsigned char *__restrict__ slices, int *__restrict__ exps)
 {
     if (*skip_if)
         return;
@@ -641,6 +641,8 @@ __global__ void k_oz_slice(const void *__restrict__ src, int64_t P, int64_t widt
     {
         const int64_t r = e % rows_pad, kg = e / rows_pad;
         const int ex = r < rows ? oz_exponent(maxbits[r]) : 0;
+        if (kg == 0)
+            exps[r] = ex;
         uint32_t packed[OZ_SLICES][4];
 #pragma unroll
         for (int j = 0; j < 8; ++j)
@@ -776,20 +778,25 @@ __global__ void __launch_bounds__(128, 1)
             full_phase[s] ^= 1u;
             pending[s] = false;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t base = smem_u32(smem + s * OZ_STAGE);
+            // the descriptor's start field is address >> 4 in its low 14 bits
+            // (shared addresses < 256 KiB), so the descriptor of a block at
+            // byte offset o from the stage is the stage's descriptor + o / 16:
+            // one add per MMA, the rest folds into constants
+            const uint64_t d0 = smem_desc(smem_u32(smem + s * OZ_STAGE), 128, OZ_SBO);
+            const uint32_t first = kc > 0 ? 1u : 0u;
 #pragma unroll
             for (int L = 2; L <= OZ_LMAX; ++L)
             {
+                constexpr int kA = OZ_A_BLOCK / 16, kB = OZ_B_BLOCK / 16, kB0 = OZ_SLICES * OZ_A_BLOCK / 16;
                 const int s_lo = L - OZ_SLICES > 1 ? L - OZ_SLICES : 1;
                 const int s_hi = L - 1 < OZ_SLICES ? L - 1 : OZ_SLICES;
+#pragma unroll
                 for (int sa = s_lo; sa <= s_hi; ++sa)
                 {
                     const int sb = L - sa;
-                    const uint64_t da = smem_desc(base + (uint32_t)((sa - 1) * OZ_A_BLOCK), 128, OZ_SBO);
-                    const uint64_t db =
-                        smem_desc(base + (uint32_t)(OZ_SLICES * OZ_A_BLOCK + (sb - 1) * OZ_B_BLOCK), 128, OZ_SBO);
-                    const uint32_t acc = (kc > 0 || sa > s_lo) ? 1u : 0u;
-                    mma_bf16(tmem + (uint32_t)((L - 2) * OZ_TN), da, db, acc);
+                    const uint64_t da = d0 + (uint64_t)((sa - 1) * kA);
+                    const uint64_t db = d0 + (uint64_t)(kB0 + (sb - 1) * kB);
+                    mma_bf16(tmem + (uint32_t)((L - 2) * OZ_TN), da, db, sa > s_lo ? 1u : first);
                 }
             }
             mma_commit(&empty[s]);
@@ -880,11 +887,29 @@ __global__ void __launch_bounds__(128, 1)
                      : "memory");
 }
 
-// out[k][t] += (sum_z C[z][k][t], sum_z C[z][K+k][t]) * 2^(e_row + e_col - 12)
+// (h, l) += (bh, bl) in double-float (TwoSum, then the low parts)
+__device__ __forceinline__ void oz_df_add(float &h, float &l, float bh, float bl)
+{
+    const float s = __fadd_rn(h, bh);
+    const float bb = __fsub_rn(s, h);
+    const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(bh, bb));
+    h = s;
+    l = __fadd_rn(l, __fadd_rn(err, bl));
+}
+
+// v * 2^e, exact: the power of two from its bits when it is a normal double
+__device__ __forceinline__ double oz_scale(double v, int e)
+{
+    if (e >= -1022 && e <= 1023)
+        return v * __longlong_as_double((long long)(e + 1023) << 52);
+    return ldexp(v, e);
+}
+
+// out[k][t] += (sum_z C[z][k][t], sum_z C[z][K+k][t]) * 2^(e_row + e_col - 12);
+// segments summed in double-float, float64 only for the scale and the add
 __global__ void k_oz_finish(const float2 *__restrict__ C, int64_t nseg, int64_t seg_stride, int64_t cols_pad,
-                            int64_t K, int64_t S, const unsigned long long *__restrict__ max_a,
-                            const unsigned long long *__restrict__ max_b, const int *__restrict__ skip_if,
-                            double2 *__restrict__ out)
+                            int64_t K, int64_t S, const int *__restrict__ exp_a, const int *__restrict__ exp_b,
+                            const int *__restrict__ skip_if, double2 *__restrict__ out)
 {
     if (*skip_if)
         return;
@@ -892,18 +917,18 @@ __global__ void k_oz_finish(const float2 *__restrict__ C, int64_t nseg, int64_t 
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
     {
         const int64_t k = e / S, t = e - k * S;
-        const int eb = oz_exponent(max_b[t]);
-        double re = 0.0, im = 0.0;
-        for (int64_t z = 0; z < nseg; ++z)
+        const float2 *ca = C + k * cols_pad + t, *cb = C + (K + k) * cols_pad + t;
+        float2 a = ca[0], b = cb[0];
+        for (int64_t z = 1; z < nseg; ++z)
         {
-            const float2 a = C[z * seg_stride + k * cols_pad + t];
-            const float2 b = C[z * seg_stride + (K + k) * cols_pad + t];
-            re += (double)a.x + (double)a.y;
-            im += (double)b.x + (double)b.y;
+            const float2 a2 = ca[z * seg_stride], b2 = cb[z * seg_stride];
+            oz_df_add(a.x, a.y, a2.x, a2.y);
+            oz_df_add(b.x, b.y, b2.x, b2.y);
         }
+        const int eb = exp_b[t] - 12;
         double2 o = out[e];
-        o.x += ldexp(re, oz_exponent(max_a[k]) + eb - 12);
-        o.y += ldexp(im, oz_exponent(max_a[K + k]) + eb - 12);
+        o.x += oz_scale((double)a.x + (double)a.y, exp_a[k] + eb);
+        o.y += oz_scale((double)b.x + (double)b.y, exp_a[K + k] + eb);
         out[e] = o;
     }
 }
@@ -912,6 +937,7 @@ struct OzLayout
 {
     int64_t Mp, Np, Kp, kchunks, nseg;
     unsigned long long *max_a, *max_b;
+    int *exp_a, *exp_b;
     unsigned char *a_sl, *b_sl;
     float2 *C;
 };
@@ -928,6 +954,9 @@ OzLayout oz_layout(int64_t M, int64_t N, int64_t Kd, void *ws)
     g.max_a = (unsigned long long *)p;
     g.max_b = g.max_a + g.Mp;
     p += round_up((g.Mp + g.Np) * 8, 256);
+    g.exp_a = (int *)p;
+    g.exp_b = g.exp_a + g.Mp;
+    p += round_up((g.Mp + g.Np) * 4, 256);
     g.a_sl = p;
     p += OZ_SLICES * g.Mp * g.Kp * 2;
     g.b_sl = p;
@@ -941,7 +970,8 @@ OzLayout oz_layout(int64_t M, int64_t N, int64_t Kd, void *ws)
 size_t oz_workspace_bytes(int64_t M, int64_t N, int64_t Kd)
 {
     const OzLayout g = oz_layout(M, N, Kd, nullptr);
-    return (size_t)(round_up((g.Mp + g.Np) * 8, 256) + OZ_SLICES * (g.Mp + g.Np) * g.Kp * 2 +
+    return (size_t)(round_up((g.Mp + g.Np) * 8, 256) + round_up((g.Mp + g.Np) * 4, 256) +
+                    OZ_SLICES * (g.Mp + g.Np) * g.Kp * 2 +
                     g.nseg * g.Mp * g.Np * 8) +
            256;
 }
@@ -955,7 +985,7 @@ cudaError_t launch_contract_oz_expect(const void *H, const double *E, int64_t P,
     cudaError_t e;
     if ((e = cudaMemsetAsync(g.max_a, 0, (size_t)(g.Mp + g.Np) * 8, st)))
         return e;
-    const int64_t rows_per_block = P > 32 * 4096 ? (P + 4095) / 4096 : 32; // grid y <= 4096
+    const int64_t rows_per_block = P > 8 * 4096 ? (P + 4095) / 4096 : 8; // grid y <= 4096
     const unsigned py = (unsigned)((P + rows_per_block - 1) / rows_per_block);
     k_oz_max_h<<<dim3((unsigned)((K + 127) / 128), py), 128, 0, st>>>((const double2 *)H, P, K, rows_per_block,
                                                                       g.max_a, flag);
@@ -965,11 +995,11 @@ cudaError_t launch_contract_oz_expect(const void *H, const double *E, int64_t P,
     if ((e = launched()))
         return e;
     k_oz_slice<true><<<grid_for(g.Mp * (g.Kp / 8)), 256, 0, st>>>(H, P, K, 2 * K, g.Mp, g.Kp, OZ_TM, g.max_a, flag,
-                                                                  g.a_sl);
+                                                                  g.a_sl, g.exp_a);
     if ((e = launched()))
         return e;
     k_oz_slice<false><<<grid_for(g.Np * (g.Kp / 8)), 256, 0, st>>>(E, P, S, S, g.Np, g.Kp, OZ_TN, g.max_b, flag,
-                                                                   g.b_sl);
+                                                                   g.b_sl, g.exp_b);
     if ((e = launched()))
         return e;
     if ((e = cudaFuncSetAttribute(k_gemm_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM)))
@@ -979,7 +1009,7 @@ cudaError_t launch_contract_oz_expect(const void *H, const double *E, int64_t P,
                                           flag);
     if ((e = launched()))
         return e;
-    k_oz_finish<<<grid_for(K * S), 256, 0, st>>>(g.C, g.nseg, g.Mp * g.Np, g.Np, K, S, g.max_a, g.max_b, flag,
+    k_oz_finish<<<grid_for(K * S), 256, 0, st>>>(g.C, g.nseg, g.Mp * g.Np, g.Np, K, S, g.exp_a, g.exp_b, flag,
                                                  (double2 *)out);
     return launched();
 }

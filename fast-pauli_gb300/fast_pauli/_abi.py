@@ -54,6 +54,7 @@ SIGNATURES = {
     "fpg_summed_expect": (ctypes.c_int, [_P, _P, _I64, _P, _P, _I64, _I32, _P]),
     "fpg_summed_apply": (ctypes.c_int, [_P, _P, _I64, _P, _P, _I64, _I32, _P]),
     "fpg_summed_apply_weighted": (ctypes.c_int, [_P, _P, _I64, _P, _P, _P, _I64, _I32, _P]),
+    "fpg_op_product": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _PI64, _P]),
     "fpg_summed_square": (ctypes.c_int, [_P, _P, _I64, _P, _P, _I32, _P]),
     "fpg_to_tensor": (ctypes.c_int, [_P, _P, _I64, _P, _I32, _P]),
     "fpg_summed_expect_noalloc": (ctypes.c_int, [ctypes.c_char_p, _I64, _I32, _P, _I64, _P, _P, _I64, _I32, _P]),

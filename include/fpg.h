@@ -168,6 +168,23 @@ int fpg_summed_apply_weighted(const fpg_operator *op, const void *coeffs, int64_
                               const void *data, void *out, int64_t n_states, int32_t dtype, void *stream);
 
 /*
+ * Product of two operators with equal strings merged:
+ *   (sum_i coeffs_a(i) A_i) (sum_j coeffs_b(j) B_j) = sum_k c_k C_k
+ * over the distinct strings C_k among the products A_i B_j.  Replaces
+ * PauliOp operator* (__pauli_op.hpp:237-281) and PauliString::operator*
+ * (__pauli_string.hpp:228-247) inside it.  coeffs_a (n_strings(a)) and
+ * coeffs_b (n_strings(b)) are complex128 device arrays; the results go to
+ * device arrays of n_strings(a) * n_strings(b) entries: out_x, out_z the
+ * (x, z) masks of C_k (bit n-1-q is character q: I (0,0), X (1,0), Y (1,1),
+ * Z (0,1)), sorted by (x, z), and out_coeffs the complex128 c_k; *n_out
+ * (host) receives the number of distinct strings.  Coefficients are summed
+ * in pair order (i, j), so results are deterministic.  Synchronises
+ * `stream`.  FPG_ERR_UNSUPPORTED when n_strings(a) * n_strings(b) >= 2^31.
+ */
+int fpg_op_product(const fpg_operator *a, const void *coeffs_a, const fpg_operator *b, const void *coeffs_b,
+                   uint64_t *out_x, uint64_t *out_z, void *out_coeffs, int64_t *n_out, void *stream);
+
+/*
  * Coefficients of the squares A_k^2 of a SummedPauliOp's operators
  * A_k = sum_j coeffs(j,k) P_j:
  *   out(a,k) = sum_{i,j: P_i P_j = phase * Q_a} phase * coeffs(i,k) * coeffs(j,k)
