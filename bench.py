@@ -576,6 +576,65 @@ def run_square(args):
                              "kind": "port", "sample": f"all {P}^2 pairs, {Ks} of {K} operators ({tc:.2f} s)"}}
 
 
+def run_product(args):
+    """PauliOp @ PauliOp with equal strings merged (fpg_op_product): the
+    configuration-2 operator set (n=14, 861 weight<=2 strings) times itself
+    with seeded complex coefficients, 741321 string pairs -> the distinct
+    strings of weight <= 4.  Metric: string pairs/s."""
+    import numpy as np
+    import torch
+
+    import fast_pauli as fp
+    import oracle
+    from fast_pauli import _abi
+
+    torch.cuda.set_device(0)
+    n = 14
+    strings = [str(s) for s in fp.helpers.calculate_pauli_strings_max_weight(n, 2)][1:]
+    P = len(strings)
+    rng = np.random.default_rng(1005)
+    c = rng.standard_normal(P) + 1j * rng.standard_normal(P)
+    L = _abi.lib()
+    op = _abi.Operator(strings)
+    stream = _stream_handle()
+    dc = torch.from_numpy(c).cuda()
+    N = P * P
+    ox = torch.empty(N, dtype=torch.int64, device="cuda")
+    oz = torch.empty(N, dtype=torch.int64, device="cuda")
+    oc = torch.empty(N, dtype=torch.complex128, device="cuda")
+    n_out = ctypes.c_int64(0)
+
+    def step():
+        _abi.check(L.fpg_op_product(op.handle, dc.data_ptr(), op.handle, dc.data_ptr(), ox.data_ptr(), oz.data_ptr(),
+                                    oc.data_ptr(), ctypes.byref(n_out), stream))
+
+    n0 = _abi.kernel_launches()
+    t = time_device(step, args.steps, args.warmup)
+    launches = (_abi.kernel_launches() - n0) / (args.steps + args.warmup)
+    # end to end: the public API (host coefficients and strings in, host PauliOp out)
+    a = fp.PauliOp(list(c), strings)
+    a @ a
+    t0 = time.perf_counter()
+    res = a @ a
+    t_e2e = time.perf_counter() - t0
+    # CPU baseline and parity: the oracle's restatement of the reference's
+    # product, all pairs
+    tc = time.perf_counter()
+    want = oracle.op_product(c, strings, c, strings)
+    tc = time.perf_counter() - tc
+    got = dict(zip(res.pauli_strings_as_str, res.coeffs))
+    err = max(abs(got[s] - w) for s, w in want.items()) / max(abs(w) for w in want.values())
+    same = sorted(got) == sorted(want)
+    return {"metric": "product string-pairs/s", "value": N / t, "unit": "string-pairs/s",
+            "workload": f"PauliOp @ PauliOp float64: n={n}, {P} x {P} weight<=2 strings -> {n_out.value} distinct",
+            "ms_per_step": t * 1e3, "steps": args.steps, "warmup": args.warmup, "launches_per_step": launches,
+            "e2e": {"value": N / t_e2e, "unit": "string-pairs/s", "ms": t_e2e * 1e3, "h2d_bytes": P * 16,
+                    "d2h_bytes": int(n_out.value) * 32, "api": "fast_pauli.PauliOp.__matmul__"},
+            "parity_vs_oracle": {"same_strings": same, "max_rel_err": float(err)},
+            "cpu_baseline": {"value": N / tc, "unit": "string-pairs/s", "cores": 1, "kind": "port",
+                             "sample": f"all {N} pairs ({tc:.2f} s, one hash map, serial)"}}
+
+
 def _square_dev(L, _abi, strings, h, sq_strings, stream):
     import torch
 
@@ -790,7 +849,7 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-mixed", action="store_true")
-    ap.add_argument("--workload", default="summed", choices=["summed", "batch", "serve", "square", "to_tensor"],
+    ap.add_argument("--workload", default="summed", choices=["summed", "batch", "serve", "square", "to_tensor", "product"],
                     help="summed: configuration 2 (default line); batch: configuration 4; serve: configuration 5; "
                          "square: SummedPauliOp.square of the configuration-2 operators")
     ap.add_argument("--requests", type=int, default=60, help="serve: requests per rate")
@@ -809,7 +868,7 @@ def main():
     if args.workload != "summed" and args.impl == "ours":
         if rank == 0:
             line = {"batch": run_batch, "serve": run_serve, "square": run_square,
-                    "to_tensor": run_to_tensor}[args.workload](args)
+                    "to_tensor": run_to_tensor, "product": run_product}[args.workload](args)
             print(json.dumps(line), flush=True)
         return
     if args.impl == "reference":

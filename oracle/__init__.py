@@ -73,6 +73,8 @@ def lib() -> ctypes.CDLL:
         L.fpo_summed_square.argtypes = [P, i64, ci, P, i64, P, i64, P]
         L.fpo_summed_square.restype = ci
         L.fpo_summed_to_tensor.argtypes = [P, i64, ci, P, i64, P]
+        L.fpo_op_product.argtypes = [P, P, i64, P, P, i64, ci, P, P]
+        L.fpo_op_product.restype = i64
         L.fpo_max_threads.restype = ci
         _lib = L
     return _lib
@@ -258,6 +260,23 @@ def summed_square(strings, h, sq_strings) -> np.ndarray:
     if rc != 0:
         raise ValueError("a product of two strings is not among the squared strings")
     return out
+
+
+def op_product(a_coeffs, a_strings, b_coeffs, b_strings) -> dict:
+    """PauliOp product with equal strings merged (PauliOp operator*):
+    {string: coefficient}, strings in order of first appearance."""
+    ac, n = codes_of(a_strings)
+    bc, n2 = codes_of(b_strings)
+    if n != n2:
+        raise ValueError("Mismatched dimensions for provided PauliOp")
+    a = _c(a_coeffs)
+    b = _c(b_coeffs)
+    N = len(a_strings) * len(b_strings)
+    codes = np.zeros((max(N, 1), max(n, 1)), dtype=np.uint8)
+    coeffs = np.zeros(max(N, 1), dtype=np.complex128)
+    cnt = lib().fpo_op_product(_p(ac), _p(a), len(a_strings), _p(bc), _p(b), len(b_strings), n, _p(codes), _p(coeffs))
+    letters = "IXYZ"
+    return {"".join(letters[c] for c in codes[k, :n]): coeffs[k] for k in range(cnt)}
 
 
 # --------------------------------------------------------------------------

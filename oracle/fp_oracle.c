@@ -449,6 +449,64 @@ int fpo_summed_square(const uint8_t *codes, int64_t P, int n, const double *h, i
 }
 
 /*
+ * fpo_op_product <- PauliOp operator* (__pauli_op.hpp:237-281) with the
+ * products of PauliString::operator* (__pauli_string.hpp:228-247): every
+ * pair (i, j) in order, the product string position by position with the
+ * Pauli table's phase, its coefficient phase * a_i * b_j added to the
+ * string's entry in a hash map (one map, so equal strings always merge;
+ * the reference keeps one map per OpenMP thread).  Writes the distinct
+ * strings in order of first appearance to out_codes (n codes each) and
+ * their coefficients to out_c (complex); both hold Pa * Pb entries.
+ * Returns the number of distinct strings.
+ */
+int64_t fpo_op_product(const uint8_t *a_codes, const double *a_c, int64_t Pa, const uint8_t *b_codes,
+                       const double *b_c, int64_t Pb, int n, uint8_t *out_codes, double *out_c)
+{
+    const int64_t N = Pa * Pb;
+    if (N <= 0)
+        return 0;
+    int64_t cap = 1;
+    while (cap < 2 * N)
+        cap <<= 1;
+    int64_t *slot = (int64_t *)malloc((size_t)cap * sizeof(int64_t));
+    for (int64_t s = 0; s < cap; ++s)
+        slot[s] = -1;
+    uint8_t *prod = (uint8_t *)malloc((size_t)(n > 0 ? n : 1));
+    static const double ph_re[4] = {1, 0, -1, 0}, ph_im[4] = {0, 1, 0, -1};
+    int64_t count = 0;
+    for (int64_t i = 0; i < Pa; ++i)
+        for (int64_t j = 0; j < Pb; ++j)
+        {
+            int e = 0;
+            for (int q = 0; q < n; ++q)
+            {
+                const uint8_t x = a_codes[i * n + q], y = b_codes[j * n + q];
+                e += k_pow_i[x][y];
+                prod[q] = (uint8_t)(x ^ y);
+            }
+            double ar, ai, cr, ci;
+            cmul(ph_re[e & 3], ph_im[e & 3], a_c[2 * i], a_c[2 * i + 1], &ar, &ai);
+            cmul(ar, ai, b_c[2 * j], b_c[2 * j + 1], &cr, &ci);
+            int64_t s = (int64_t)(hash_codes(prod, n) & (uint64_t)(cap - 1));
+            while (slot[s] >= 0 && memcmp(out_codes + slot[s] * n, prod, (size_t)n) != 0)
+                s = (s + 1) & (cap - 1);
+            if (slot[s] < 0)
+            {
+                slot[s] = count;
+                memcpy(out_codes + count * n, prod, (size_t)n);
+                out_c[2 * count] = 0.0;
+                out_c[2 * count + 1] = 0.0;
+                ++count;
+            }
+            out_c[2 * slot[s]] += cr;
+            out_c[2 * slot[s] + 1] += ci;
+        }
+    free(prod);
+    free(slot);
+    return count;
+}
+
+/*
  * fpo_summed_to_tensor <- SummedPauliOp::to_tensor (__summed_pauli_op.hpp:644-665):
  * out (K, D, D) complex, accumulated: for every string its sparse pattern,
  * then out(k, j, cols[j]) += h(i, k) * vals[j], strings in order, OpenMP over

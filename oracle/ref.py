@@ -49,6 +49,8 @@ def lib() -> ctypes.CDLL:
         L.fpref_pauli_strings_max_weight.restype = i64
         L.fpref_summed_square.argtypes = [ctypes.c_char_p, i64, ci, P, i64, ctypes.c_char_p, P]
         L.fpref_summed_square.restype = i64
+        L.fpref_op_product.argtypes = [ctypes.c_char_p, P, i64, ctypes.c_char_p, P, i64, ci, ctypes.c_char_p, P]
+        L.fpref_op_product.restype = i64
         _lib = L
     return _lib
 
@@ -166,3 +168,18 @@ def summed_square(strings, h):
     lib().fpref_summed_square(b, P, n, _p(h), K, sbuf, _p(out_h))
     raw = sbuf.raw[: cnt * n].decode()
     return [raw[j * n : (j + 1) * n] for j in range(cnt)], out_h
+
+
+def op_product(a_coeffs, a_strings, b_coeffs, b_strings):
+    """The reference's PauliOp operator*: (strings, coefficients) as it
+    returns them (one entry per string per OpenMP thread map)."""
+    ab, n = _join(a_strings)
+    bb, _ = _join(b_strings)
+    a = _c(a_coeffs)
+    b = _c(b_coeffs)
+    cnt = lib().fpref_op_product(ab, _p(a), len(a_strings), bb, _p(b), len(b_strings), n, None, None)
+    sbuf = ctypes.create_string_buffer(int(cnt) * n + 1)
+    out = np.zeros(cnt, dtype=np.complex128)
+    lib().fpref_op_product(ab, _p(a), len(a_strings), bb, _p(b), len(b_strings), n, sbuf, _p(out))
+    raw = sbuf.raw[: cnt * n].decode()
+    return [raw[j * n : (j + 1) * n] for j in range(cnt)], out

@@ -149,6 +149,23 @@ extern "C"
     }
 
     // SummedPauliOp::square: returns the new string count; writes strings and (P2 x K) coeffs when buffers given
+    // PauliOp operator* of the reference; with out_strs == nullptr only the
+    // number of result terms (one entry per string per OpenMP thread map)
+    int64_t fpref_op_product(const char *a_strs, const double *a_c, int64_t Pa, const char *b_strs,
+                             const double *b_c, int64_t Pb, int n, char *out_strs, double *out_c)
+    {
+        std::vector<cd> ca((cd *)a_c, (cd *)a_c + Pa), cb((cd *)b_c, (cd *)b_c + Pb);
+        fp::PauliOp<double> a(ca, parse(a_strs, Pa, n)), b(cb, parse(b_strs, Pb, n));
+        auto r = a * b;
+        if (out_strs)
+            for (size_t j = 0; j < r.pauli_strings.size(); ++j)
+                for (int q = 0; q < n; ++q)
+                    out_strs[j * n + q] = "IXYZ"[r.pauli_strings[j].paulis[q].code];
+        if (out_c)
+            std::memcpy(out_c, r.coeffs.data(), r.coeffs.size() * sizeof(cd));
+        return (int64_t)r.pauli_strings.size();
+    }
+
     int64_t fpref_summed_square(const char *strs, int64_t P, int n, const double *h, int64_t K, char *out_strs,
                                 double *out_h)
     {

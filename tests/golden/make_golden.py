@@ -123,6 +123,23 @@ def main() -> None:
         os.path.join(HERE, "summed_square_n6.npz"),
         strings=_s(strings), h=h, sq_strings=_s(sq_strings), sq_h=sq_h,
     )
+    # --- PauliOp products (next row): random operators and a self-product
+    # with many equal strings; the reference's raw output (its per-thread maps
+    # may list a string more than once)
+    rng = np.random.default_rng(11)
+    a_s = [str(x) for x in oracle.uniform_strings(rng, 5, 12)]
+    b_s = [str(x) for x in oracle.uniform_strings(rng, 5, 9)]
+    a_c = rng.standard_normal(12) + 1j * rng.standard_normal(12)
+    b_c = rng.standard_normal(9) + 1j * rng.standard_normal(9)
+    ab_s, ab_c = ref.op_product(a_c, a_s, b_c, b_s)
+    w2 = ref.pauli_strings_max_weight(4, 2)
+    w_c = rng.standard_normal(len(w2)) + 1j * rng.standard_normal(len(w2))
+    ww_s, ww_c = ref.op_product(w_c, w2, w_c, w2)
+    np.savez_compressed(
+        os.path.join(HERE, "op_product.npz"),
+        a_strings=_s(a_s), a_coeffs=a_c, b_strings=_s(b_s), b_coeffs=b_c, ab_strings=_s(ab_s), ab_coeffs=ab_c,
+        w_strings=_s(w2), w_coeffs=w_c, ww_strings=_s(ww_s), ww_coeffs=ww_c,
+    )
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 import oracle
+from conftest import golden
 
 pytestmark = pytest.mark.gpu
 
@@ -21,6 +22,10 @@ def _dense_op(op):
     for c, s in zip(op.coeffs, op.pauli_strings_as_str):
         m += c * oracle.dense(s)
     return m
+
+
+def _strs(a):
+    return [str(x) for x in a]
 
 
 def _masks(s):
@@ -79,6 +84,25 @@ def test_product_reference_cases():
     np.testing.assert_allclose(_dense_op(l_op @ r_op @ l_op @ r_op), want, atol=1e-11)
 
 
+@pytest.mark.parametrize("case", ["ab", "ww"])
+def test_product_vs_reference_golden(case):
+    # the reference's output (tests/golden/op_product.npz) lists a string once
+    # per OpenMP thread map; merged it must equal ours, where each string
+    # appears once
+    g = golden("op_product.npz")
+    a = ("a", "b") if case == "ab" else ("w", "w")
+    got = fp.PauliOp(list(g[f"{a[0]}_coeffs"]), _strs(g[f"{a[0]}_strings"])) @ fp.PauliOp(
+        list(g[f"{a[1]}_coeffs"]), _strs(g[f"{a[1]}_strings"])
+    )
+    want = {}
+    for s, c in zip(_strs(g[f"{case}_strings"]), g[f"{case}_coeffs"]):
+        want[s] = want.get(s, 0) + c
+    strs = got.pauli_strings_as_str
+    assert len(set(strs)) == len(strs) and sorted(strs) == sorted(want)
+    g_c = dict(zip(strs, got.coeffs))
+    assert max(abs(g_c[s] - want[s]) for s in want) < 1e-12
+
+
 @pytest.mark.parametrize("n,Pa,Pb", [(10, 300, 200), (40, 50, 40), (33, 60, 70)])
 def test_product_matches_pairwise_products(n, Pa, Pb):
     """Sizes past the dense check, keys wider than 64 bits (n > 32), repeated
@@ -90,6 +114,8 @@ def test_product_matches_pairwise_products(n, Pa, Pb):
     as_[3] = as_[1]  # a repeated string
     got = fp.PauliOp(list(ac), as_) @ fp.PauliOp(list(bc), bs)
     want = _pairwise(ac, as_, bc, bs)
+    orc = oracle.op_product(ac, as_, bc, bs)
+    assert max(abs(orc[s] - want[s]) for s in want) <= 1e-12 * max(1.0, max(abs(v) for v in want.values()))
     strs = got.pauli_strings_as_str
     assert sorted(strs) == sorted(want)
     keys = [_masks(s) for s in strs]

@@ -126,3 +126,36 @@ def test_restatement_matches_reference_when_present(ref_available):
     assert normwise(oracle.summed_expectation(strings, h, psi), ref.summed_expectation(strings, h, psi)) < 1e-14
     assert normwise(oracle.summed_apply_weighted(strings, h, psi, data),
                     ref.summed_apply_weighted(strings, h, psi, data)) < 1e-14
+
+
+def _merged(strings, coeffs):
+    d = {}
+    for s, c in zip(strings, coeffs):
+        d[str(s)] = d.get(str(s), 0) + c
+    return d
+
+
+@pytest.mark.parametrize("case", ["ab", "ww"])
+def test_op_product_golden(case):
+    # the reference's PauliOp operator* lists a string once per OpenMP thread
+    # map; merged, it must equal the oracle's single map
+    g = golden("op_product.npz")
+    if case == "ab":
+        got = oracle.op_product(g["a_coeffs"], g["a_strings"], g["b_coeffs"], g["b_strings"])
+    else:
+        got = oracle.op_product(g["w_coeffs"], g["w_strings"], g["w_coeffs"], g["w_strings"])
+    want = _merged(g[f"{case}_strings"], g[f"{case}_coeffs"])
+    assert sorted(got) == sorted(want)
+    assert max(abs(got[s] - want[s]) for s in want) < 1e-12
+
+
+def test_op_product_matches_dense():
+    rng = np.random.default_rng(12)
+    for n in (1, 2, 3):
+        a_s, b_s = oracle.uniform_strings(rng, n, 5), oracle.uniform_strings(rng, n, 4)
+        a_c = rng.standard_normal(5) + 1j * rng.standard_normal(5)
+        b_c = rng.standard_normal(4) + 1j * rng.standard_normal(4)
+        got = oracle.op_product(a_c, a_s, b_c, b_s)
+        m = sum(c * oracle.dense(s) for s, c in got.items())
+        want = sum(c * oracle.dense(s) for s, c in zip(a_s, a_c)) @ sum(c * oracle.dense(s) for s, c in zip(b_s, b_c))
+        np.testing.assert_allclose(m, want, atol=1e-13)
