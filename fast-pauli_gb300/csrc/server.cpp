@@ -13,10 +13,14 @@
 //    admits every request that fits (smaller ones may pass a large one that
 //    does not fit yet).  A request larger than the whole budget is refused at
 //    submission (FPG_ERR_BUSY).
-//  * Priorities: half of the slots are streams of the device's highest
-//    priority, reserved for small requests (<= kSmallWork amplitude-terms);
-//    the block scheduler starts their CTAs ahead of the large requests' as
-//    SMs free up, so short requests are not stuck behind long ones.
+//  * Priorities: requests fall in three classes by work (amplitude-terms
+//    n_strings * 2^n * n_states): small (<= kSmallWork, milliseconds), medium
+//    (<= kMediumWork, up to ~0.2 s) and large.  The slots are split into
+//    three tiers of streams at the device's highest, middle and lowest
+//    priority; a request takes a free slot of its own tier, else of a lower
+//    tier, never of a higher one.  The block scheduler starts the CTAs of
+//    higher-priority streams first as SMs free up, so short requests are not
+//    stuck behind long ones and medium ones not behind the largest.
 //  * Continuous: the scheduler thread admits new requests the moment slots
 //    and memory free up, while earlier requests are still running; admitted
 //    requests run concurrently on their slots' streams, so their kernels
@@ -62,13 +66,18 @@ struct Ticket
     std::string err;
     clock_type::time_point t_submit, t_start, t_done;
     int slot = -1;
-    bool small = false; // work <= kSmallWork amplitude-terms
+    int tier = 2; // 0 small, 1 medium, 2 large
 };
 
-// Requests of at most this many amplitude-terms (n_strings * 2^n * n_states,
-// a few milliseconds of GPU time) count as small and run on high-priority
-// slots.
+// Work classes in amplitude-terms (n_strings * 2^n * n_states): small is a
+// few milliseconds of GPU time, medium up to ~0.2 s.
 constexpr double kSmallWork = 4.0e9;
+constexpr double kMediumWork = 2.0e11;
+
+int work_tier(double work)
+{
+    return work <= kSmallWork ? 0 : (work <= kMediumWork ? 1 : 2);
+}
 
 } // namespace
 
@@ -87,7 +96,7 @@ struct fpg_server
         cudaEvent_t event = nullptr;
         uint64_t ticket = 0;
         bool busy = false;
-        bool high = false; // created with the device's highest stream priority
+        int tier = 2; // 0: the device's highest stream priority, 1: middle, 2: lowest
     };
     std::vector<Slot> slots;
     size_t reserved = 0;
@@ -174,14 +183,12 @@ void fpg_server::run()
         for (auto it = queue.begin(); it != queue.end();)
         {
             Ticket &t = tickets[*it];
-            // small requests take a high-priority slot when one is free (else any
-            // free slot); large ones only normal slots, so that small requests
-            // always find a stream whose work the GPU schedules first
+            // a free slot of the request's tier, else of a lower-priority tier:
+            // higher tiers stay free for the shorter requests
             auto free_slot = slots.end();
-            if (t.small)
-                free_slot = std::find_if(slots.begin(), slots.end(), [](const Slot &s) { return !s.busy && s.high; });
-            if (free_slot == slots.end())
-                free_slot = std::find_if(slots.begin(), slots.end(), [](const Slot &s) { return !s.busy && !s.high; });
+            for (int tier = t.tier; tier <= 2 && free_slot == slots.end(); ++tier)
+                free_slot = std::find_if(slots.begin(), slots.end(),
+                                         [tier](const Slot &s) { return !s.busy && s.tier == tier; });
             if (free_slot == slots.end())
             {
                 ++it; // no slot of its class: later requests of the other class may pass
@@ -253,18 +260,24 @@ extern "C"
             s->cfg.max_queue = 1 << 20;
         cudaError_t e = cudaGetDevice(&s->device);
         s->slots.resize((size_t)config->n_slots);
-        // the first half of the slots (none when there is one) run at the
-        // highest stream priority and serve small requests
+        // tiers: a third of the slots each for medium and large requests (at
+        // least one large slot), the rest for small ones; a single slot is a
+        // large-tier slot, which every request may take.  Stream priorities:
+        // highest / middle / lowest of the device's range
         int prio_low = 0, prio_high = 0;
         if (e == cudaSuccess)
             e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
-        const int n_high = config->n_slots > 1 ? config->n_slots / 2 : 0;
+        const int n = config->n_slots;
+        const int n_large = n > 1 ? std::max(1, n / 3) : 1;
+        const int n_medium = n > 2 ? std::max(1, n / 3) : 0;
+        const int n_small = n - n_large - n_medium;
+        const int prio_of[3] = {prio_high, (prio_high + prio_low) / 2, prio_low};
         for (size_t i = 0; i < s->slots.size(); ++i)
         {
             auto &sl = s->slots[i];
-            sl.high = (int)i < n_high;
+            sl.tier = (int)i < n_small ? 0 : ((int)i < n_small + n_medium ? 1 : 2);
             if (e == cudaSuccess)
-                e = cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking, sl.high ? prio_high : prio_low);
+                e = cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking, prio_of[sl.tier]);
             if (e == cudaSuccess)
                 e = cudaEventCreateWithFlags(&sl.event, cudaEventDisableTiming);
         }
@@ -320,7 +333,7 @@ extern "C"
             int32_t nq = 0;
             int64_t ps = 0;
             fpg_operator_info(req->op, &nq, &ps, nullptr);
-            t.small = (double)ps * std::ldexp(1.0, nq) * (double)req->n_states <= kSmallWork;
+            t.tier = work_tier((double)ps * std::ldexp(1.0, nq) * (double)req->n_states);
         }
         t.t_submit = clock_type::now();
         s->tickets.emplace(id, std::move(t));
