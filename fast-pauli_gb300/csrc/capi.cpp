@@ -482,6 +482,41 @@ int64_t family_partials(const fpg_operator *op, const ExpectPlan &plan, int64_t 
     return total;
 }
 
+// The apply stage.  float32 as is; float64 in df64 on the float32 pipes:
+// state and coefficients split once (and range-checked) into df64 copies,
+// the df64 kernel, then the float64 kernel, which returns at once unless a
+// value lay outside the df64 range (the df64 kernel then did nothing).
+// n_cw: complex coefficients in cw (P, or P * S when weighted).
+size_t apply_scratch_bytes(int n, int64_t S, int64_t n_cw, bool fp32)
+{
+    const int64_t n_elem = ((int64_t)1 << n) * S;
+    if (fp32 || n_elem * 16 > kDfSplitMaxBytes)
+        return 0;
+    return 256 + (size_t)n_elem * 16 + (size_t)n_cw * 16;
+}
+
+int run_apply(bool fp32, bool weighted, const DevOp &dop, const void *cw, int64_t n_cw, const void *states, void *out,
+              int64_t S, cudaStream_t st)
+{
+    const size_t bytes = apply_scratch_bytes(dop.n, S, n_cw, fp32);
+    if (bytes == 0)
+    {
+        FPG_CUDA(launch_apply(fp32, weighted, dop, cw, states, out, S, st));
+        return FPG_OK;
+    }
+    Scratch sc(st);
+    FPG_CUDA(sc.alloc(bytes));
+    int *flag = (int *)sc.p;
+    void *psi_df = (char *)sc.p + 256;
+    void *cw_df = (char *)psi_df + (((int64_t)1 << dop.n) * S) * 16;
+    FPG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    FPG_CUDA(launch_df_split(states, ((int64_t)1 << dop.n) * S, psi_df, flag, st));
+    FPG_CUDA(launch_df_split(cw, n_cw, cw_df, flag, st));
+    FPG_CUDA(launch_apply_df(weighted, dop, cw_df, psi_df, out, S, flag, st));
+    FPG_CUDA(launch_apply(false, weighted, dop, cw, states, out, S, st, flag));
+    return FPG_OK;
+}
+
 int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int64_t S, bool fp32, cudaStream_t st)
 {
     if (S <= 0 || op->P <= 0)
@@ -570,7 +605,7 @@ size_t request_scratch_bytes(const fpg_operator *op, int64_t K, int64_t S, bool 
     if (weighted)
     {
         const size_t csz = fp32 ? 8 : 16;
-        size_t b = 2 * P * (size_t)S * csz;
+        size_t b = 2 * P * (size_t)S * csz + apply_scratch_bytes(op->n, S, op->P * S, fp32);
         if (fp32)
             b += tc_workspace_bytes(2 * op->P, S, K);
         return b + 4096;
@@ -923,8 +958,7 @@ extern "C"
         FPG_CUDA(cw.alloc((size_t)op->P * csz));
         const DevOp dop = op->dev();
         FPG_CUDA(launch_prep_coeffs(fp32, dop, coeffs, 0, cw.p, st));
-        FPG_CUDA(launch_apply(fp32, false, dop, cw.p, states, out, n_states, st));
-        return FPG_OK;
+        return run_apply(fp32, false, dop, cw.p, op->P, states, out, n_states, st);
     }
 
     int fpg_summed_apply(const fpg_operator *op, const void *coeffs, int64_t n_operators, const void *states,
@@ -952,8 +986,7 @@ extern "C"
         FPG_CUDA(cw.alloc((size_t)op->P * csz));
         const DevOp dop = op->dev();
         FPG_CUDA(launch_prep_coeffs(fp32, dop, coeffs, n_operators, cw.p, st));
-        FPG_CUDA(launch_apply(fp32, false, dop, cw.p, states, out, n_states, st));
-        return FPG_OK;
+        return run_apply(fp32, false, dop, cw.p, op->P, states, out, n_states, st);
     }
 
     int fpg_summed_apply_weighted(const fpg_operator *op, const void *coeffs, int64_t n_operators,
@@ -992,8 +1025,7 @@ extern "C"
         else
             FPG_CUDA(launch_weighted_coeffs(fp32, coeffs, data, op->P, n_operators, n_states, w.p, st));
         FPG_CUDA(launch_prep_weighted(fp32, dop, w.p, n_states, cw.p, st));
-        FPG_CUDA(launch_apply(fp32, true, dop, cw.p, states, out, n_states, st));
-        return FPG_OK;
+        return run_apply(fp32, true, dop, cw.p, op->P * n_states, states, out, n_states, st);
     }
 
     int fpg_to_tensor(const fpg_operator *op, const void *coeffs, int64_t n_operators, void *out, int32_t dtype,

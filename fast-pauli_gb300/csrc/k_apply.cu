@@ -16,6 +16,7 @@
 // For apply_weighted the diagonal also depends on the column:
 // w(j,t) (-i)^{nY_j} replaces c_j (-i)^{nY_j}.
 #include "common.cuh"
+#include "df64.cuh"
 
 namespace fpg
 {
@@ -86,11 +87,16 @@ __global__ void k_prep_weighted(const StringRec *__restrict__ recs, const int32_
 
 constexpr int kApplyRows = 8; // output rows per thread
 
+// only_if: when not null, the launch is the float64 form behind the df64
+// kernel and returns at once unless *only_if is set.
 template <typename T, bool WEIGHTED>
 __global__ void __launch_bounds__(256)
     k_apply(const T *__restrict__ psi, T *__restrict__ out, int64_t S, int n, const Group *__restrict__ groups,
-            int64_t G, const StringRec *__restrict__ recs, const typename C2<T>::type *__restrict__ cw, int TC)
+            int64_t G, const StringRec *__restrict__ recs, const typename C2<T>::type *__restrict__ cw, int TC,
+            const int *__restrict__ only_if)
 {
+    if (only_if && *only_if == 0)
+        return;
     using CT = typename C2<T>::type;
     const int tid = threadIdx.x;
     const int tc = tid & (TC - 1);
@@ -159,6 +165,101 @@ __global__ void __launch_bounds__(256)
             CT cur = *o;
             cur.x += accr[k];
             cur.y += acci[k];
+            *o = cur;
+        }
+}
+
+constexpr int kApplyRowsDf = 4; // output rows per thread, df64 form
+
+// float64 apply in df64 on the float32 pipes (df64.cuh): the same sums as
+// k_apply<double> with amplitudes and coefficients taken from their df64
+// copies (float4 per complex value, split once per call); every product is
+// exact (FMA error terms), every sum a TwoSum, the running sums are
+// renormalised every 16 groups, and out += sum in float64 at the end.  Error
+// ~2^-46 of sum |terms|.  Returns at once when *skip_if is set (an amplitude
+// or coefficient outside the df64 range): k_apply<double> runs instead.
+template <bool WEIGHTED>
+__global__ void __launch_bounds__(256)
+    k_apply_df(const float4 *__restrict__ psi, double *__restrict__ out, int64_t S, int n,
+               const Group *__restrict__ groups, int64_t G, const StringRec *__restrict__ recs,
+               const float4 *__restrict__ cw, int TC, const int *__restrict__ skip_if)
+{
+    if (*skip_if)
+        return;
+    constexpr int R = kApplyRowsDf;
+    const int tid = threadIdx.x;
+    const int tc = tid & (TC - 1);
+    const int tr = tid / TC;
+    const int TR = blockDim.x / TC;
+    const uint64_t D = 1ull << n;
+    const uint64_t i0 = ((uint64_t)blockIdx.x * TR + tr) * R;
+    const int64_t t = (int64_t)blockIdx.y * TC + tc;
+    if (i0 >= D || t >= S)
+        return;
+    // running sums [row][h/l]
+    float ar[R][2], ai[R][2];
+#pragma unroll
+    for (int k = 0; k < R; ++k)
+        ar[k][0] = ar[k][1] = ai[k][0] = ai[k][1] = 0.f;
+    for (int64_t g = 0; g < G; ++g)
+    {
+        const Group gr = groups[g];
+        float4 b[R];
+#pragma unroll
+        for (int k = 0; k < R; ++k)
+            b[k] = i0 + k < D ? __ldg(psi + (int64_t)((i0 + k) ^ gr.x) * S + t) : make_float4(0.f, 0.f, 0.f, 0.f);
+        // diagonal of the group per row: sum of +-c over its strings (df64)
+        float wr[R][2], wi[R][2];
+        {
+            const uint64_t z = recs[gr.begin].z;
+            const float4 c = WEIGHTED ? cw[(int64_t)gr.begin * S + t] : cw[gr.begin];
+#pragma unroll
+            for (int k = 0; k < R; ++k)
+            {
+                const float sg = (__popcll((i0 + k) & z) & 1) ? -1.f : 1.f;
+                wr[k][0] = sg * c.x;
+                wr[k][1] = sg * c.y;
+                wi[k][0] = sg * c.z;
+                wi[k][1] = sg * c.w;
+            }
+        }
+        for (int32_t s = gr.begin + 1; s < gr.begin + gr.count; ++s)
+        {
+            const uint64_t z = recs[s].z;
+            const float4 c = WEIGHTED ? cw[(int64_t)s * S + t] : cw[s];
+#pragma unroll
+            for (int k = 0; k < R; ++k)
+            {
+                const float sg = (__popcll((i0 + k) & z) & 1) ? -1.f : 1.f;
+                df_add(wr[k][0], wr[k][1], sg * c.x, sg * c.y);
+                df_add(wi[k][0], wi[k][1], sg * c.z, sg * c.w);
+            }
+        }
+        // sum += w * b  (complex, df64)
+#pragma unroll
+        for (int k = 0; k < R; ++k)
+        {
+            df_fma(wr[k][0], wr[k][1], b[k].x, b[k].y, ar[k][0], ar[k][1]);
+            df_fma(-wi[k][0], -wi[k][1], b[k].z, b[k].w, ar[k][0], ar[k][1]);
+            df_fma(wr[k][0], wr[k][1], b[k].z, b[k].w, ai[k][0], ai[k][1]);
+            df_fma(wi[k][0], wi[k][1], b[k].x, b[k].y, ai[k][0], ai[k][1]);
+        }
+        if ((g & 15) == 15)
+#pragma unroll
+            for (int k = 0; k < R; ++k)
+            {
+                df_norm(ar[k][0], ar[k][1]);
+                df_norm(ai[k][0], ai[k][1]);
+            }
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k)
+        if (i0 + k < D)
+        {
+            double2 *o = reinterpret_cast<double2 *>(out) + (int64_t)(i0 + k) * S + t;
+            double2 cur = *o;
+            cur.x += df_to_double(ar[k][0], ar[k][1]);
+            cur.y += df_to_double(ai[k][0], ai[k][1]);
             *o = cur;
         }
 }
@@ -252,12 +353,25 @@ cudaError_t launch_prep_weighted(bool fp32, const DevOp &op, const void *W, int6
     return launched();
 }
 
+// Column lanes of an apply launch: up to 32, fewer while a column tile (all
+// 2^n rows x TC columns, the rows the groups' partners i ^ x_g are gathered
+// from) would not stay in L2 -- down to 64-byte row segments.  CTAs run in
+// column-tile order, so the gathers of one tile then hit L2.
+constexpr int64_t kApplyTileBytes = int64_t(48) << 20;
+int apply_lanes(int64_t S, int n, int esz)
+{
+    int tc = pick_tc(S);
+    while (tc * esz > 64 && ((int64_t(1) << n) * tc * esz) > kApplyTileBytes)
+        tc >>= 1;
+    return tc;
+}
+
 cudaError_t launch_apply(bool fp32, bool weighted, const DevOp &op, const void *cw, const void *psi, void *out,
-                         int64_t S, cudaStream_t st)
+                         int64_t S, cudaStream_t st, const int *only_if)
 {
     if (S <= 0 || op.G <= 0)
         return cudaSuccess;
-    const int TC = pick_tc(S);
+    const int TC = apply_lanes(S, op.n, fp32 ? 8 : 16);
     const int TR = 256 / TC;
     const uint64_t D = 1ull << op.n;
     const uint64_t rows_per_cta = (uint64_t)TR * kApplyRows;
@@ -266,20 +380,39 @@ cudaError_t launch_apply(bool fp32, bool weighted, const DevOp &op, const void *
     {
         if (weighted)
             k_apply<float, true><<<grid, 256, 0, st>>>((const float *)psi, (float *)out, S, op.n, op.groups, op.G,
-                                                       op.recs, (const float2 *)cw, TC);
+                                                       op.recs, (const float2 *)cw, TC, only_if);
         else
             k_apply<float, false><<<grid, 256, 0, st>>>((const float *)psi, (float *)out, S, op.n, op.groups, op.G,
-                                                        op.recs, (const float2 *)cw, TC);
+                                                        op.recs, (const float2 *)cw, TC, only_if);
     }
     else
     {
         if (weighted)
             k_apply<double, true><<<grid, 256, 0, st>>>((const double *)psi, (double *)out, S, op.n, op.groups, op.G,
-                                                        op.recs, (const double2 *)cw, TC);
+                                                        op.recs, (const double2 *)cw, TC, only_if);
         else
             k_apply<double, false><<<grid, 256, 0, st>>>((const double *)psi, (double *)out, S, op.n, op.groups,
-                                                         op.G, op.recs, (const double2 *)cw, TC);
+                                                         op.G, op.recs, (const double2 *)cw, TC, only_if);
     }
+    return launched();
+}
+
+cudaError_t launch_apply_df(bool weighted, const DevOp &op, const void *cw_df, const void *psi_df, void *out,
+                            int64_t S, const int *skip_if, cudaStream_t st)
+{
+    if (S <= 0 || op.G <= 0)
+        return cudaSuccess;
+    const int TC = apply_lanes(S, op.n, 16);
+    const int TR = 256 / TC;
+    const uint64_t D = 1ull << op.n;
+    const uint64_t rows_per_cta = (uint64_t)TR * kApplyRowsDf;
+    dim3 grid((unsigned)((D + rows_per_cta - 1) / rows_per_cta), (unsigned)((S + TC - 1) / TC));
+    if (weighted)
+        k_apply_df<true><<<grid, 256, 0, st>>>((const float4 *)psi_df, (double *)out, S, op.n, op.groups, op.G,
+                                               op.recs, (const float4 *)cw_df, TC, skip_if);
+    else
+        k_apply_df<false><<<grid, 256, 0, st>>>((const float4 *)psi_df, (double *)out, S, op.n, op.groups, op.G,
+                                                op.recs, (const float4 *)cw_df, TC, skip_if);
     return launched();
 }
 

@@ -264,6 +264,41 @@ def test_float64_path_far_from_unit_scale(scale_psi, scale_h):
     assert normwise(got, want) < TOL_C128
 
 
+@pytest.mark.parametrize("scale_psi,scale_h", [(1.0, 1.0), (1e-30, 1.0), (1e15, 1.0), (1.0, 1e20), (1.0, 1e-35)])
+def test_float64_apply_far_from_unit_scale(scale_psi, scale_h):
+    """The float64 apply runs in double-float arithmetic on the float32 pipes
+    when states and coefficients lie within 2^-90 .. 2^40 and in float64
+    otherwise (the double-float kernel then leaves the output untouched)."""
+    rng = np.random.default_rng(64)
+    n, S, K = 8, 40, 3
+    strings = oracle.uniform_strings(rng, n, 50) + oracle.calculate_pauli_strings_max_weight(n, 1)[1:]
+    P = len(strings)
+    h = (rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))) * scale_h
+    psi = oracle.unit_norm_states(rng, 1 << n, S) * scale_psi
+    data = rng.standard_normal((K, S))
+    coeffs = h[:, 0]
+    op = fp.PauliOp(coeffs, strings)
+    sop = fp.SummedPauliOp(strings, h)
+    assert normwise(op.apply(psi), oracle.op_apply(strings, coeffs, psi)) < TOL_C128
+    assert normwise(sop.apply(psi), oracle.summed_apply(strings, h, psi)) < TOL_C128
+    assert normwise(sop.apply_weighted(psi, data), oracle.summed_apply_weighted(strings, h, psi, data)) < TOL_C128
+    # accumulating into a non-zero output (+=) through the C ABI path
+    torch = pytest.importorskip("torch")
+    from fast_pauli import _abi
+
+    L = _abi.lib()
+    o = _abi.Operator(strings)
+    dpsi = torch.from_numpy(psi).cuda()
+    dc = torch.from_numpy(np.ascontiguousarray(coeffs)).cuda()
+    base = oracle.unit_norm_states(rng, 1 << n, S) * scale_psi
+    out = torch.from_numpy(base.copy()).cuda()
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _abi.check(L.fpg_apply(o.handle, dc.data_ptr(), dpsi.data_ptr(), out.data_ptr(), S, _abi.FPG_C128, st))
+    torch.cuda.synchronize()
+    assert normwise(out.cpu().numpy(), base + oracle.op_apply(strings, coeffs, psi)) < TOL_C128
+    o.close()
+
+
 def test_float64_contraction_mixed_magnitudes():
     """The float64 contraction scales every row of H^T and of the per-string
     expectation table by a power of two and multiplies digit slices on the
@@ -597,7 +632,8 @@ def test_config2_full_size_properties():
     applied = op.apply(psi)
     via_apply = torch.einsum("it,it->t", psi.conj(), applied).cpu().numpy()
     assert normwise(op.expectation_value(psi).cpu().numpy(), via_apply) < 1e-12
-    # P^2 = I for a single string
+    # P^2 = I for a single string (to the double-float representation of the
+    # amplitudes, 48 significand bits: ~2^-48 relative)
     s = fp.PauliString("XYZI" * 3 + "YZ")
     back = s.apply(s.apply(psi))
-    assert normwise(back.cpu().numpy(), psi.cpu().numpy()) < 1e-15
+    assert normwise(back.cpu().numpy(), psi.cpu().numpy()) < 1e-14
