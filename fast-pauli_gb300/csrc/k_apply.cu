@@ -87,6 +87,16 @@ __global__ void k_prep_weighted(const StringRec *__restrict__ recs, const int32_
 
 constexpr int kApplyRows = 8; // output rows per thread
 
+// Bit k = parity(popcount((i0 + k) & z)) for the rows i0 .. i0+31 of a
+// thread (i0 a multiple of the rows per thread, so all in one 32-row block):
+// the string's parity table of the low five row bits, flipped by the parity
+// of the high bits -- one popcount per string instead of one per row.
+__device__ __forceinline__ uint32_t sign_bits(const StringRec &rec, uint64_t i0)
+{
+    const uint32_t hi = (uint32_t)(__popcll(i0 & rec.z & ~31ull) & 1);
+    return (rec.mask_lo >> (uint32_t)(i0 & 31u)) ^ (0u - hi);
+}
+
 // only_if: when not null, the launch is the float64 form behind the df64
 // kernel and returns at once unless *only_if is set.
 template <typename T, bool WEIGHTED>
@@ -132,12 +142,12 @@ __global__ void __launch_bounds__(256)
             wr[k] = wi[k] = T(0);
         for (int32_t s = gr.begin; s < gr.begin + gr.count; ++s)
         {
-            const uint64_t z = recs[s].z;
+            const uint32_t sb = sign_bits(recs[s], i0);
             const CT c = WEIGHTED ? cw[(int64_t)s * S + t] : cw[s];
 #pragma unroll
             for (int k = 0; k < kApplyRows; ++k)
             {
-                if (__popcll((i0 + k) & z) & 1)
+                if ((sb >> k) & 1u)
                 {
                     wr[k] -= c.x;
                     wi[k] -= c.y;
@@ -211,12 +221,12 @@ __global__ void __launch_bounds__(256)
         // diagonal of the group per row: sum of +-c over its strings (df64)
         float wr[R][2], wi[R][2];
         {
-            const uint64_t z = recs[gr.begin].z;
+            const uint32_t sb = sign_bits(recs[gr.begin], i0);
             const float4 c = WEIGHTED ? cw[(int64_t)gr.begin * S + t] : cw[gr.begin];
 #pragma unroll
             for (int k = 0; k < R; ++k)
             {
-                const float sg = (__popcll((i0 + k) & z) & 1) ? -1.f : 1.f;
+                const float sg = ((sb >> k) & 1u) ? -1.f : 1.f;
                 wr[k][0] = sg * c.x;
                 wr[k][1] = sg * c.y;
                 wi[k][0] = sg * c.z;
@@ -225,12 +235,12 @@ __global__ void __launch_bounds__(256)
         }
         for (int32_t s = gr.begin + 1; s < gr.begin + gr.count; ++s)
         {
-            const uint64_t z = recs[s].z;
+            const uint32_t sb = sign_bits(recs[s], i0);
             const float4 c = WEIGHTED ? cw[(int64_t)s * S + t] : cw[s];
 #pragma unroll
             for (int k = 0; k < R; ++k)
             {
-                const float sg = (__popcll((i0 + k) & z) & 1) ? -1.f : 1.f;
+                const float sg = ((sb >> k) & 1u) ? -1.f : 1.f;
                 df_add(wr[k][0], wr[k][1], sg * c.x, sg * c.y);
                 df_add(wi[k][0], wi[k][1], sg * c.z, sg * c.w);
             }
