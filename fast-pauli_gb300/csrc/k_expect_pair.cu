@@ -91,20 +91,24 @@ __device__ __forceinline__ void df_conj_mul_add(const float (&a)[4], const float
 // for the final cross-thread reduction.  Error <= ~2^-46 of sum |terms|.
 // An amplitude outside the df64 range raises *range_flag (df64.cuh); with
 // PRE the state comes split already (and checked) by k_df_split.
-template <bool PRE>
+template <bool PRE, int V>
 __global__ void __launch_bounds__(256, 2)
     k_expect_pair_df(const void *__restrict__ psi, int64_t S, int n, const StringRec *__restrict__ recs,
                      const int32_t *__restrict__ orig, int64_t P, const PairChunk *__restrict__ chunks, int TC,
                      int n_splits, double *__restrict__ out, int *__restrict__ range_flag)
 {
+    static_assert(V == 1 || PRE, "two columns per thread read the split copy");
+    // rows per load batch: four with one column, two with two (the same
+    // bytes in flight, half the row-index work per column)
+    constexpr int NB4 = V == 1 ? 4 : 2;
     bool bad = false;
-    extern __shared__ double red[]; // blockDim.x doubles
+    extern __shared__ double red[]; // blockDim.x * V doubles
     const PairChunk ch = chunks[blockIdx.x];
     const int tid = threadIdx.x;
     const int tc = tid & (TC - 1);
     const int tr = tid / TC;
     const int TR = blockDim.x / TC;
-    const int64_t t0 = (int64_t)blockIdx.z * TC + tc;
+    const int64_t t0 = ((int64_t)blockIdx.z * TC + tc) * V; // S % V == 0
     const bool col_ok = t0 < S;
 
     const uint64_t D = 1ull << n;
@@ -125,8 +129,13 @@ __global__ void __launch_bounds__(256, 2)
     const int e2 = split_in_block && pl >= 0 ? max(abit, pl) : -1;
     const int n_rows = 32 >> ((e1 >= 0) + (e2 >= 0));
 
-    // running df64 sums [c][h/l]: U_c^re, U_c^im
-    float ure[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, uim[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    // running df64 sums [column][c][h/l]: U_c^re, U_c^im
+    float ure[V][2][2], uim[V][2][2];
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+            ure[v][c][0] = ure[v][c][1] = uim[v][c][0] = uim[v][c][1] = 0.f;
     if (col_ok)
     {
         for (int64_t m = b0 + tr; m < b1; m += TR)
@@ -135,15 +144,20 @@ __global__ void __launch_bounds__(256, 2)
             const uint64_t beta = paired ? (((um >> hb) << (hb + 1)) | (um & ((1ull << hb) - 1ull))) : um;
             const uint64_t base = beta << 5;
             const uint64_t baseB = base ^ xh;
-            float sre[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, sim[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
-            // four visited rows at a time, all their loads issued before any use
-            // (the kernel is bound by L2 latency); n_rows is 8, 16 or 32
-            for (int m0 = 0; m0 < n_rows; m0 += 4)
-            {
-                uint32_t r0[4];
-                bool ok[4];
+            float sre[V][2][2], sim[V][2][2];
 #pragma unroll
-                for (int u = 0; u < 4; ++u)
+            for (int v = 0; v < V; ++v)
+#pragma unroll
+                for (int c = 0; c < 2; ++c)
+                    sre[v][c][0] = sre[v][c][1] = sim[v][c][0] = sim[v][c][1] = 0.f;
+            // NB4 visited rows at a time, all their loads issued before any
+            // use (the kernel is bound by L2 latency); n_rows is 8, 16 or 32
+            for (int m0 = 0; m0 < n_rows; m0 += NB4)
+            {
+                uint32_t r0[NB4];
+                bool ok[NB4];
+#pragma unroll
+                for (int u = 0; u < NB4; ++u)
                 {
                     uint32_t r = (uint32_t)(m0 + u);
                     if (e1 >= 0)
@@ -153,51 +167,63 @@ __global__ void __launch_bounds__(256, 2)
                     r0[u] = r;
                     ok[u] = (int)r < RB;
                 }
-                float a[4][4], b[4][4];
+                float a[NB4][V][4], b[NB4][V][4];
 #pragma unroll
-                for (int u = 0; u < 4; ++u)
+                for (int u = 0; u < NB4; ++u)
                     if (ok[u])
                     {
-                        load_df<PRE>(psi, (int64_t)(base + r0[u]) * S + t0, a[u], bad);
-                        load_df<PRE>(psi, (int64_t)(baseB + (r0[u] ^ xl)) * S + t0, b[u], bad);
+                        const int64_t ea = (int64_t)(base + r0[u]) * S + t0;
+                        const int64_t eb = (int64_t)(baseB + (r0[u] ^ xl)) * S + t0;
+#pragma unroll
+                        for (int v = 0; v < V; ++v)
+                        {
+                            load_df<PRE>(psi, ea + v, a[u][v], bad);
+                            load_df<PRE>(psi, eb + v, b[u][v], bad);
+                        }
                     }
                 if (split_in_block)
                 {
                     // rows r1 = r0 | 2^a (< RB as a < n)
-                    float c[4][4], d[4][4];
+                    float c[NB4][V][4], d[NB4][V][4];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u)
+                    for (int u = 0; u < NB4; ++u)
                         if (ok[u])
                         {
                             const uint32_t r1 = r0[u] | (1u << abit);
-                            load_df<PRE>(psi, (int64_t)(base + r1) * S + t0, c[u], bad);
-                            load_df<PRE>(psi, (int64_t)(baseB + (r1 ^ xl)) * S + t0, d[u], bad);
+                            const int64_t ec = (int64_t)(base + r1) * S + t0;
+                            const int64_t ed = (int64_t)(baseB + (r1 ^ xl)) * S + t0;
+#pragma unroll
+                            for (int v = 0; v < V; ++v)
+                            {
+                                load_df<PRE>(psi, ec + v, c[u][v], bad);
+                                load_df<PRE>(psi, ed + v, d[u][v], bad);
+                            }
                         }
 #pragma unroll
-                    for (int u = 0; u < 4; ++u)
+                    for (int u = 0; u < NB4; ++u)
                         if (ok[u])
-                            df_conj_mul_add(c[u], d[u], sre[1], sim[1]);
+#pragma unroll
+                            for (int v = 0; v < V; ++v)
+                                df_conj_mul_add(c[u][v], d[u][v], sre[v][1], sim[v][1]);
                 }
 #pragma unroll
-                for (int u = 0; u < 4; ++u)
+                for (int u = 0; u < NB4; ++u)
                     if (ok[u])
-                        df_conj_mul_add(a[u], b[u], sre[0], sim[0]);
+#pragma unroll
+                        for (int v = 0; v < V; ++v)
+                            df_conj_mul_add(a[u][v], b[u][v], sre[v][0], sim[v][0]);
             }
             const int c0 = (abit >= 5) ? (int)((base >> abit) & 1u) : 0;
-            if (c0 == 0)
+#pragma unroll
+            for (int v = 0; v < V; ++v)
             {
-                df_add(ure[0][0], ure[0][1], sre[0][0], sre[0][1]);
-                df_add(uim[0][0], uim[0][1], sim[0][0], sim[0][1]);
-            }
-            else
-            {
-                df_add(ure[1][0], ure[1][1], sre[0][0], sre[0][1]);
-                df_add(uim[1][0], uim[1][1], sim[0][0], sim[0][1]);
-            }
-            if (split_in_block)
-            {
-                df_add(ure[1][0], ure[1][1], sre[1][0], sre[1][1]);
-                df_add(uim[1][0], uim[1][1], sim[1][0], sim[1][1]);
+                df_add(ure[v][c0][0], ure[v][c0][1], sre[v][0][0], sre[v][0][1]);
+                df_add(uim[v][c0][0], uim[v][c0][1], sim[v][0][0], sim[v][0][1]);
+                if (split_in_block)
+                {
+                    df_add(ure[v][1][0], ure[v][1][1], sre[v][1][0], sre[v][1][1]);
+                    df_add(uim[v][1][0], uim[v][1][1], sim[v][1][0], sim[v][1][1]);
+                }
             }
         }
     }
@@ -205,20 +231,28 @@ __global__ void __launch_bounds__(256, 2)
     if (!PRE && bad)
         atomicOr(range_flag, 1);
     // float64 reduction of the four sums over the row lanes (fixed order)
-    double tot[4];
+    double tot[4][V];
 #pragma unroll
     for (int q = 0; q < 4; ++q)
     {
-        const float *u = q == 0 ? ure[0] : q == 1 ? ure[1] : q == 2 ? uim[0] : uim[1];
-        red[tr * TC + tc] = df_to_double(u[0], u[1]);
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+        {
+            const float *u = q == 0 ? ure[v][0] : q == 1 ? ure[v][1] : q == 2 ? uim[v][0] : uim[v][1];
+            red[(tr * TC + tc) * V + v] = df_to_double(u[0], u[1]);
+        }
         __syncthreads();
         for (int s = TR >> 1; s > 0; s >>= 1)
         {
             if (tr < s)
-                red[tr * TC + tc] += red[(tr + s) * TC + tc];
+#pragma unroll
+                for (int v = 0; v < V; ++v)
+                    red[(tr * TC + tc) * V + v] += red[((tr + s) * TC + tc) * V + v];
             __syncthreads();
         }
-        tot[q] = red[tc];
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+            tot[q][v] = red[tc * V + v];
         __syncthreads();
     }
     if (tr != 0 || !col_ok)
@@ -232,9 +266,14 @@ __global__ void __launch_bounds__(256, 2)
         const bool flip = ((rec.z & ~pbit) != 0);
         const int ny = (int)(rec.meta & 3u);
         const double f = ((ny & 2) ? -1.0 : 1.0) * (pbit ? 2.0 : 1.0);
-        const double u0 = odd ? tot[2] : tot[0];
-        const double u1 = odd ? tot[3] : tot[1];
-        out[((int64_t)blockIdx.y * P + orig[sidx]) * S + t0] = f * (flip ? u0 - u1 : u0 + u1);
+        double *dst = out + ((int64_t)blockIdx.y * P + orig[sidx]) * S + t0;
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+        {
+            const double u0 = odd ? tot[2][v] : tot[0][v];
+            const double u1 = odd ? tot[3][v] : tot[1][v];
+            dst[v] = f * (flip ? u0 - u1 : u0 + u1);
+        }
     }
 }
 
@@ -437,13 +476,19 @@ cudaError_t launch_expect_pair(bool fp32, const void *psi, int64_t S, int n, con
     const size_t smem = 256 * plan.V * sizeof(double);
     if (!fp32)
     {
-        // df64 on the float32 pipes, then the float64 form for out-of-range inputs
-        if (psi_df)
-            k_expect_pair_df<true><<<grid, 256, smem, st>>>(psi_df, S, n, op.recs, op.orig, op.P, d_chunks, plan.TC,
-                                                            plan.n_splits, out, range_flag);
+        // df64 on the float32 pipes, then the float64 form for out-of-range
+        // inputs.  With the split copy and an even number of states, two
+        // adjacent columns per thread (half the column lanes, the same column
+        // tile): half the row-index work per column.
+        if (psi_df && S % 2 == 0 && plan.TC >= 2)
+            k_expect_pair_df<true, 2><<<grid, 256, 2 * smem, st>>>(psi_df, S, n, op.recs, op.orig, op.P, d_chunks,
+                                                                   plan.TC / 2, plan.n_splits, out, range_flag);
+        else if (psi_df)
+            k_expect_pair_df<true, 1><<<grid, 256, smem, st>>>(psi_df, S, n, op.recs, op.orig, op.P, d_chunks,
+                                                               plan.TC, plan.n_splits, out, range_flag);
         else
-            k_expect_pair_df<false><<<grid, 256, smem, st>>>(psi, S, n, op.recs, op.orig, op.P, d_chunks, plan.TC,
-                                                             plan.n_splits, out, range_flag);
+            k_expect_pair_df<false, 1><<<grid, 256, smem, st>>>(psi, S, n, op.recs, op.orig, op.P, d_chunks, plan.TC,
+                                                                plan.n_splits, out, range_flag);
         if (cudaError_t e = launched())
             return e;
         k_expect_pair<double, 1><<<grid, 256, smem, st>>>((const double *)psi, S, n, op.recs, op.orig, op.P, d_chunks,
