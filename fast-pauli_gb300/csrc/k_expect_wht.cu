@@ -234,6 +234,9 @@ __global__ void __launch_bounds__(kWhtThreads)
     uint64_t *s_z = s_base + TR;                                                   // [count] z masks of the chunk
 
     const WhtChunk ch = chunks[blockIdx.x];
+    // [count] per string: bit rr = parity(base of block rr & z), the block's
+    // sign, computed once per CTA instead of once per column lane
+    uint32_t *s_sign = reinterpret_cast<uint32_t *>(s_z + ch.count);
     const int tid = threadIdx.x;
     const int tc = tid % TC;
     const int tr = tid / TC;
@@ -327,6 +330,16 @@ __global__ void __launch_bounds__(kWhtThreads)
             s_base[tr] = base;
         __syncthreads();
         const int nb = (b1 - mr < (int64_t)TR) ? (int)(b1 - mr) : TR;
+        const bool masks = TR <= 32; // one bit per block of the round
+        for (int k = tid; masks && k < G; k += blockDim.x)
+        {
+            const uint64_t z = s_z[k];
+            uint32_t sg = 0;
+            for (int rr = 0; rr < nb; ++rr)
+                sg |= (uint32_t)(__popcll(s_base[rr] & z) & 1) << rr;
+            s_sign[k] = sg;
+        }
+        __syncthreads();
 #pragma unroll
         for (int j = 0; j < SLOTS; ++j)
         {
@@ -334,11 +347,13 @@ __global__ void __launch_bounds__(kWhtThreads)
             if (k >= G)
                 break;
             const uint64_t z = s_z[k];
+            const uint32_t sg = masks ? s_sign[k] : 0u;
             const int part = k >= ch.n_even ? 1 : 0; // odd #Y strings read the Im transform
             const cell *wp = wsm + (size_t)((part * TR * 16) + (int)(z & 15u)) * TC + tc;
             val sum = W::zero();
             for (int rr = 0; rr < nb; ++rr)
-                W::add_cell(sum, wp[(size_t)rr * 16 * TC], (__popcll(s_base[rr] & z) & 1) != 0);
+                W::add_cell(sum, wp[(size_t)rr * 16 * TC],
+                            masks ? ((sg >> rr) & 1u) != 0 : (__popcll(s_base[rr] & z) & 1) != 0);
             W::acc_add(sums[j], sum);
         }
         __syncthreads();
@@ -404,7 +419,7 @@ cudaError_t launch_expect_wht(bool fp32, const void *psi, int64_t S, int n, cons
     const int threads = kWhtThreads;
     const int TR = threads / TC;
     const int slots_needed = (max_count + TR - 1) / TR;
-    const size_t smem = (size_t)2 * TR * 16 * TC * 8 + (size_t)TR * 8 + (size_t)max_count * 8;
+    const size_t smem = (size_t)2 * TR * 16 * TC * 8 + (size_t)TR * 8 + (size_t)max_count * 12;
 #define FPG_WHT(SL, BOTH)                                                                                              \
     return launch_sl<SL, BOTH>(fp32, psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, range_flag,     \
                                psi_df, smem, st)
