@@ -76,6 +76,12 @@ struct ArF32
     {
         return (double)a.v - (double)a.c;
     }
+    // a += b (both compensated: b's sum is b.v - b.c)
+    static __device__ __forceinline__ void acc_merge(acc &a, const acc &b)
+    {
+        acc_add(a, b.v);
+        acc_add(a, -b.c);
+    }
     static __device__ __forceinline__ acc from2(float2 f)
     {
         return acc{f.x, f.y};
@@ -124,6 +130,10 @@ struct ArF64
     static __device__ __forceinline__ void acc_add(acc &a, val x)
     {
         a += x;
+    }
+    static __device__ __forceinline__ void acc_merge(acc &a, const acc &b)
+    {
+        a += b;
     }
     static __device__ __forceinline__ double to_double(const acc &a)
     {
@@ -176,6 +186,10 @@ struct ArDF
     static __device__ __forceinline__ void acc_add(acc &a, val x)
     {
         df_add(a.h, a.l, x.h, x.l);
+    }
+    static __device__ __forceinline__ void acc_merge(acc &a, const acc &b)
+    {
+        df_add(a.h, a.l, b.h, b.l);
     }
     static __device__ __forceinline__ double to_double(const acc &a)
     {
@@ -344,13 +358,43 @@ __global__ void __launch_bounds__(256, 2)
             ml[p][j] = A::acc_zero();
     }
 
+    auto base_of = [&](int64_t m) -> uint64_t {
+        const uint64_t um = (uint64_t)m;
+        const uint64_t beta = paired ? (((um >> hb) << (hb + 1)) | (um & ((1ull << hb) - 1ull))) : um;
+        return beta << 5;
+    };
+    // The high bits that change within this thread's next few blocks go to
+    // their cells block by block (lo_mask); the others hold still over runs
+    // of blocks, whose totals are summed in registers (run) and added to the
+    // cells when the pattern changes -- far fewer shared-memory updates.
+    uint64_t lo_mask = 0;
+    if (b0 + tr < b1)
+    {
+        const uint64_t f = base_of(b0 + tr);
+        for (int k = 1; k < 8 && b0 + tr + (int64_t)k * TR < b1; ++k)
+            lo_mask |= base_of(b0 + tr + (int64_t)k * TR) ^ f;
+    }
+    lo_mask &= hmask;
+    const uint64_t hi_mask = hmask & ~lo_mask;
+    auto cell_merge = [&](int p, uint64_t bits, const acc &x) {
+        for (uint64_t w = bits; w; w &= w - 1ull)
+        {
+            const int b = __ffsll((long long)w) - 1;
+            float2 *cell = smh + (p * NH + __popcll(hmask & ((1ull << b) - 1ull))) * 256 + tid;
+            acc a = A::from2(*cell);
+            A::acc_merge(a, x);
+            *cell = A::to2(a);
+        }
+    };
+    acc run[2] = {A::acc_zero(), A::acc_zero()};
+    uint64_t run_hi = 0;
+    bool in_run = false;
+
     if (col_ok)
     {
         for (int64_t m = b0 + tr; m < b1; m += TR)
         {
-            const uint64_t um = (uint64_t)m;
-            const uint64_t beta = paired ? (((um >> hb) << (hb + 1)) | (um & ((1ull << hb) - 1ull))) : um;
-            const uint64_t base = beta << 5;
+            const uint64_t base = base_of(m);
             const uint64_t baseB = base ^ xh;
             val bt[2] = {A::zero(), A::zero()};
             val bl[2][5];
@@ -363,6 +407,18 @@ __global__ void __launch_bounds__(256, 2)
                 block_marginals<A, 5>(psi, S, t0, base, baseB, xl, pl, RB, need_re, need_im, bt, bl, bad);
             else
                 block_marginals<A, 4>(psi, S, t0, base, baseB, xl, pl, RB, need_re, need_im, bt, bl, bad);
+            const uint64_t hi = base & hi_mask;
+            if (in_run && hi != run_hi)
+            {
+#pragma unroll
+                for (int p = 0; p < 2; ++p)
+                {
+                    cell_merge(p, run_hi, run[p]);
+                    run[p] = A::acc_zero();
+                }
+            }
+            in_run = true;
+            run_hi = hi;
 #pragma unroll
             for (int p = 0; p < 2; ++p)
             {
@@ -370,7 +426,8 @@ __global__ void __launch_bounds__(256, 2)
 #pragma unroll
                 for (int j = 0; j < 5; ++j)
                     A::acc_add(ml[p][j], bl[p][j]);
-                for (uint64_t w = base & hmask; w; w &= w - 1ull)
+                A::acc_add(run[p], bt[p]);
+                for (uint64_t w = base & lo_mask; w; w &= w - 1ull)
                 {
                     const int b = __ffsll((long long)w) - 1;
                     float2 *cell = smh + (p * NH + __popcll(hmask & ((1ull << b) - 1ull))) * 256 + tid;
@@ -380,6 +437,10 @@ __global__ void __launch_bounds__(256, 2)
                 }
             }
         }
+        if (in_run)
+#pragma unroll
+            for (int p = 0; p < 2; ++p)
+                cell_merge(p, run_hi, run[p]);
     }
 
     if (A::kRaises && bad)
