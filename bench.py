@@ -119,7 +119,7 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ workload
-def config2(n=14, K=1000, S=1024, seed=1002, device="cuda"):
+def weight2_problem(n=14, K=1000, S=1024, seed=1002, device="cuda"):
     import numpy as np
     import torch
 
@@ -173,7 +173,7 @@ def run_ours(args, rank, world, dist):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     n, K, S = 14, 1000, 1024
-    strings, h, psi = config2(n=n, K=K, S=S, seed=1002 + rank)
+    strings, h, psi = weight2_problem(n=n, K=K, S=S, seed=1002 + rank)
     P, D = len(strings), 1 << n
     terms = P * D * S
     L = _abi.lib()
@@ -245,7 +245,7 @@ def run_ours(args, rank, world, dist):
         "unit": "GB/s",
         "frac": alg_bytes_expect / t_expect / 1e9 / hbm,
         "peak_kind": peak_kind,
-        "traffic": _ncu_traffic("expect_stage_config2_fp64.md"),
+        "traffic": _ncu_traffic("expect_stage_n14_weight2_fp64.md"),
         "kernel": "expectation stage (fpg_expect_strings: k_expect_pair + k_expect_marg + k_expect_wht)",
         "kernel_ms": t_expect * 1e3,
         "algorithmic_bytes_per_launch": alg_bytes_expect,
@@ -332,7 +332,7 @@ def run_profile_c64(args):
     torch.cuda.set_device(0)
     if args.profile == "mixed":
         n, K, S = 18, 1000, 512
-        strings, h, psi = config2(n=n, K=K, S=S, seed=1003)
+        strings, h, psi = weight2_problem(n=n, K=K, S=S, seed=1003)
     else:
         n, K, S = 20, 1, 64
         rng = np.random.default_rng(1006)
@@ -363,7 +363,7 @@ def run_mixed(args):
     from fast_pauli import _abi
 
     n, K, S = 18, 1000, 512
-    strings, h, psi = config2(n=n, K=K, S=S, seed=1003)
+    strings, h, psi = weight2_problem(n=n, K=K, S=S, seed=1003)
     P, D = len(strings), 1 << n
     L = _abi.lib()
     op = _abi.Operator(strings)
@@ -456,7 +456,7 @@ def run_reference(args, rank, world):
 
 
 def _cfg4_problems(seed=1004, count=256):
-    """Configuration 4: n ~ U{8..20}, strings log-uniform in [16, 4096]
+    """Uneven batch: n ~ U{8..20}, strings log-uniform in [16, 4096]
     (uniform random strings), states ~ U{1..256}."""
     import numpy as np
 
@@ -486,7 +486,7 @@ def run_to_tensor(args):
 
     torch.cuda.set_device(0)
     n, K = 12, 8
-    strings, h, _ = config2(n=n, K=K, S=1, seed=1007)
+    strings, h, _ = weight2_problem(n=n, K=K, S=1, seed=1007)
     P, D = len(strings), 1 << n
     L = _abi.lib()
     op = _abi.Operator(strings)
@@ -521,7 +521,7 @@ def run_to_tensor(args):
 
 
 def run_square(args):
-    """SummedPauliOp.square of the configuration-2 operator set (n=14, 861
+    """SummedPauliOp.square of the n=14 weight<=2 operator set (861
     weight<=2 strings, K=1000) onto the 91771 strings of weight <= 4.
     Metric: pair-terms/s = P^2 * K per call / time (the reference forms every
     (i, j, k) term)."""
@@ -534,7 +534,7 @@ def run_square(args):
 
     torch.cuda.set_device(0)
     n, K = 14, 1000
-    strings, h, _ = config2(n=n, K=K, S=1, seed=1002)
+    strings, h, _ = weight2_problem(n=n, K=K, S=1, seed=1002)
     sq_strings = [str(s) for s in fp.helpers.calculate_pauli_strings_max_weight(n, 4)]
     P, A = len(strings), len(sq_strings)
     L = _abi.lib()
@@ -578,7 +578,7 @@ def run_square(args):
 
 def run_product(args):
     """PauliOp @ PauliOp with equal strings merged (fpg_op_product): the
-    configuration-2 operator set (n=14, 861 weight<=2 strings) times itself
+    n=14 weight<=2 operator set (861 strings) times itself
     with seeded complex coefficients, 741321 string pairs -> the distinct
     strings of weight <= 4.  Metric: string pairs/s."""
     import numpy as np
@@ -650,7 +650,7 @@ def _square_dev(L, _abi, strings, h, sq_strings, stream):
 
 
 def run_batch(args):
-    """Configuration 4: 256 uneven PauliOp.expectation_value problems in one
+    """Uneven batch: 256 PauliOp.expectation_value problems in one
     persistent, graph-captured launch (tuning from the autotuner, tuned on the
     problems with n <= 14) versus 256 separate plain launches."""
     import numpy as np
@@ -715,7 +715,7 @@ def run_batch(args):
         cpu_terms += len(strings) * (1 << n) * S
         err_or = max(err_or, normwise_np(items[i]["out_b"].cpu().numpy()[0], want))
     hbm, _ = _peaks()
-    return {"metric": METRIC, "workload": "config 4: 256 PauliOp.expectation_value, n~U{8..20}, P log-uniform "
+    return {"metric": METRIC, "workload": "uneven batch: 256 PauliOp.expectation_value, n~U{8..20}, P log-uniform "
                                           "16..4096 uniform strings, S~U{1..256}, complex64",
             "value": terms / t_batch, "unit": UNIT, "ms_per_step": t_batch * 1e3, "steps": args.steps,
             "plain_value": terms / t_plain, "plain_ms_per_step": t_plain * 1e3, "speedup_vs_plain": t_plain / t_batch,
@@ -735,7 +735,7 @@ def normwise_np(got, want):
 
 
 def run_serve(args):
-    """Configuration 5: Poisson arrivals of expectation_value / apply_weighted
+    """Serving: Poisson arrivals of expectation_value / apply_weighted
     requests (n ~ U{10..max_n}, strings log-uniform 32..2048, S ~ U{1..64},
     K log-uniform 1..64, complex64) against the serving loop (continuous
     admission, 8 slots, HBM budget) and against the plain per-request path
@@ -808,7 +808,7 @@ def run_serve(args):
     alone = np.array(alone)
     le20 = ns <= 20
     out = {"metric": "serving latency ms / amplitude-terms/s",
-           "workload": f"config 5: {n_req} requests per rate, Poisson rates {rates}/s, n~U{{10..{args.max_n}}}, "
+           "workload": f"serving: {n_req} requests per rate, Poisson rates {rates}/s, n~U{{10..{args.max_n}}}, "
                        "P log-uniform 32..2048 uniform strings, S~U{1..64}, K log-uniform 1..64, "
                        "50/50 expectation_value / apply_weighted, complex64",
            "service_alone_ms": {"p50": float(np.percentile(alone, 50)), "p99": float(np.percentile(alone, 99)),
@@ -843,15 +843,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--profile", nargs="?", const="summed", default=None, choices=["summed", "mixed", "random"],
-                    help="short device-only run for ncu captures: summed = configuration 2 (float64), "
+                    help="short device-only run for ncu captures: summed = the n=14 weight<=2 workload (float64), "
                          "mixed = the n=18 complex64 shape (tensor-core contraction), "
                          "random = n=20, 1024 uniform random strings, 64 states, complex64")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-mixed", action="store_true")
     ap.add_argument("--workload", default="summed", choices=["summed", "batch", "serve", "square", "to_tensor", "product"],
-                    help="summed: configuration 2 (default line); batch: configuration 4; serve: configuration 5; "
-                         "square: SummedPauliOp.square of the configuration-2 operators")
+                    help="summed: the n=14 weight<=2 SummedPauliOp workload (default line); batch: 256 uneven problems; "
+                         "serve: the request loop; "
+                         "square: SummedPauliOp.square of the n=14 weight<=2 operators")
     ap.add_argument("--requests", type=int, default=60, help="serve: requests per rate")
     ap.add_argument("--rates", default="2,4,8", help="serve: Poisson arrival rates to sweep (requests/s)")
     ap.add_argument("--max-n", type=int, default=24, help="serve: largest qubit count")

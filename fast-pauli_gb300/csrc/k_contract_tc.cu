@@ -515,9 +515,9 @@ cudaError_t launch_weighted_tc(const void *H, const float *X, int64_t P, int64_t
 //  * Epilogue: per segment, the eight exact level sums of an output are
 //    folded into a double-float value (TwoSum); the finishing kernel sums the
 //    segments in float64 and applies 2^(e_row + e_col - 12).
-// Modelled in numpy on config-2-like data (P = 861, Gaussian H, expectation
-// columns with 30x outliers): 1.4e-15 normwise against the float64 GEMM
-// (seven digits and levels up to 8: 1.6e-13).  A non-finite value
+// Modelled in numpy on data shaped like the n=14 weight<=2 workload (P = 861,
+// Gaussian H, expectation columns with 30x outliers): 1.4e-15 normwise
+// against the float64 GEMM (seven digits and levels up to 8: 1.6e-13).  A non-finite value
 // in H or E raises the call's flag instead; the float64 CUDA-core GEMM then
 // computes the contraction (every kernel here returns at once).
 namespace

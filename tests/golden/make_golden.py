@@ -56,7 +56,7 @@ def main() -> None:
         helpers[f"count_{n}_{w}"] = np.array(len(ref.pauli_strings_max_weight(n, w)))
     np.savez_compressed(os.path.join(HERE, "helpers.npz"), **helpers)
 
-    # --- configuration 1: PauliOp.apply, n=10, 64 uniform strings, 1024x100 ---
+    # --- PauliOp.apply, n=10, 64 uniform strings, 1024x100 ----------------------
     rng = np.random.default_rng(1001)
     n, P, S = 10, 64, 100
     strings = oracle.uniform_strings(rng, n, P)
@@ -64,7 +64,7 @@ def main() -> None:
     psi = oracle.unit_norm_states(rng, 1 << n, S)
     res = ref.op_apply(strings, coeffs, psi)
     np.savez_compressed(
-        os.path.join(HERE, "config1_pauli_op_apply.npz"),
+        os.path.join(HERE, "pauli_op_apply_n10.npz"),
         strings=_s(strings), coeffs=coeffs, states=psi, out=res,
     )
 
@@ -91,7 +91,7 @@ def main() -> None:
     )
     np.savez_compressed(os.path.join(HERE, "small_methods.npz"), **small)
 
-    # --- configuration-2 shape at a reduced size: weight<=2 strings minus the
+    # --- SummedPauliOp.expectation_value on weight<=2 strings minus the
     #     identity, n=8, K=20, S=16, h ~ CN(0, 1/P) --------------------------------
     rng = np.random.default_rng(1002)
     n, K, S = 8, 20, 16
@@ -100,7 +100,7 @@ def main() -> None:
     h = (rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))) / np.sqrt(2 * P)
     psi = oracle.unit_norm_states(rng, 1 << n, S)
     np.savez_compressed(
-        os.path.join(HERE, "config2_reduced_summed_expectation.npz"),
+        os.path.join(HERE, "summed_expectation_weight2_n8.npz"),
         strings=_s(strings), h=h, states=psi, out=ref.summed_expectation(strings, h, psi),
     )
 

@@ -1,7 +1,7 @@
 """GPU parity: the CUDA path against the reference's golden outputs and the CPU
 oracle on the same seeded inputs (float64 path within 1e-12 normwise relative;
 index/sign/phase work bit-exact), plus size-independent properties at the
-full configuration-2 size.  Everything runs through libfpg's C ABI: via the
+full size of the n=14 weight<=2 workload.  Everything runs through libfpg's C ABI: via the
 Python module (C++ host API -> C ABI) or directly via ctypes."""
 
 from __future__ import annotations
@@ -34,8 +34,8 @@ def test_sparse_repr_bit_exact_vs_reference():
         np.testing.assert_array_equal(np.array(vals), g[f"vals_{s}"])
 
 
-def test_config1_pauli_op_apply_vs_reference():
-    g = golden("config1_pauli_op_apply.npz")
+def test_pauli_op_apply_n10_vs_reference():
+    g = golden("pauli_op_apply_n10.npz")
     got = fp.PauliOp(g["coeffs"], _strs(g["strings"])).apply(g["states"])
     assert got.shape == (1024, 100) and got.dtype == np.complex128
     assert normwise(got, g["out"]) < TOL_C128
@@ -62,8 +62,8 @@ def test_small_methods_vs_reference():
         assert normwise(v, g[k]) < TOL_C128, (k, normwise(v, g[k]))
 
 
-def test_config2_reduced_vs_reference():
-    g = golden("config2_reduced_summed_expectation.npz")
+def test_summed_expectation_weight2_n8_vs_reference():
+    g = golden("summed_expectation_weight2_n8.npz")
     got = fp.SummedPauliOp(_strs(g["strings"]), g["h"]).expectation_value(g["states"])
     assert normwise(got, g["out"]) < TOL_C128
 
@@ -93,7 +93,7 @@ def test_uniform_strings_all_methods(n, S):
 @pytest.mark.parametrize("n", [5, 6, 8, 11])
 @pytest.mark.parametrize("S", [1, 16, 40])
 def test_weight2_strings_summed_expectation(n, S):
-    # the configuration-2 string set (all weight <= 2 strings minus the
+    # the weight <= 2 string set (all weight <= 2 strings minus the
     # identity): large x-groups, mixed #Y parities, paired and unpaired rows
     rng = np.random.default_rng(7 * n + S)
     strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
@@ -603,10 +603,10 @@ def test_c_abi_direct_device_buffers():
     op.close()
 
 
-# ------------------------------------------- full-size properties (config 2)
+# ---------------------- full-size properties (n=14, weight <= 2, 1024 states)
 
 
-def test_config2_full_size_properties():
+def test_weight2_n14_full_size_properties():
     """n=14, all 861 weight<=2 strings, S=1024 (the bench workload's shape,
     K reduced): size-independent properties instead of the oracle."""
     torch = pytest.importorskip("torch")

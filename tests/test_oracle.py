@@ -47,8 +47,8 @@ def test_helper_ordering_known_answers():
             assert len(oracle.calculate_pauli_strings_max_weight(int(n), int(w))) == int(g[key])
 
 
-def test_config1_golden():
-    g = golden("config1_pauli_op_apply.npz")
+def test_pauli_op_apply_n10_golden():
+    g = golden("pauli_op_apply_n10.npz")
     got = oracle.op_apply([str(s) for s in g["strings"]], g["coeffs"], g["states"])
     assert normwise(got, g["out"]) < 1e-14
 
@@ -97,8 +97,8 @@ def test_summed_square_missing_product_is_reported():
         oracle.summed_square(["XI", "IZ"], np.ones((2, 1)), ["II", "XI", "IZ"])  # XZ missing
 
 
-def test_config2_reduced_golden():
-    g = golden("config2_reduced_summed_expectation.npz")
+def test_summed_expectation_weight2_n8_golden():
+    g = golden("summed_expectation_weight2_n8.npz")
     got = oracle.summed_expectation([str(x) for x in g["strings"]], g["h"], g["states"])
     assert normwise(got, g["out"]) < 1e-14
 
