@@ -1255,13 +1255,24 @@ template <std::floating_point T> struct SummedPauliOp
     }
     template <typename C> detail::DevBuf upload_coeffs(cudaStream_t st) const
     {
-        // A pageable-source cudaMemcpyAsync returns once the source has been
-        // staged, so the temporary host vector may go out of scope.
-        std::vector<C> c(coeffs_raw.begin(), coeffs_raw.end());
-        detail::DevBuf d(c.size() * sizeof(C), st);
-        if (d.bytes)
+        detail::DevBuf d(coeffs_raw.size() * sizeof(C), st);
+        if (!d.bytes)
+            return d;
+        if constexpr (std::is_same_v<C, std::complex<T>>)
+        {
+            // the stored coefficients as they are (a pageable-source copy
+            // returns once the source has been staged)
+            detail::cuda_check(cudaMemcpyAsync(d.p, coeffs_raw.data(), d.bytes, cudaMemcpyHostToDevice, st),
+                               "cudaMemcpyAsync");
+        }
+        else
+        {
+            // converted first; the temporary may go out of scope once the
+            // pageable-source copy has returned
+            std::vector<C> c(coeffs_raw.begin(), coeffs_raw.end());
             detail::cuda_check(cudaMemcpyAsync(d.p, c.data(), d.bytes, cudaMemcpyHostToDevice, st),
                                "cudaMemcpyAsync");
+        }
         return d;
     }
 };

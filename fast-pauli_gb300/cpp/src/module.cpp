@@ -203,8 +203,13 @@ Arr new_zeros(const Arr &like, const std::vector<size_t> &shape)
     }
     else
     {
-        py::array_t<cd> arr(std::vector<py::ssize_t>(shape.begin(), shape.end()));
-        std::memset(arr.mutable_data(), 0, arr.nbytes());
+        // numpy.zeros: calloc'd, so a large result is zero pages until the
+        // device-to-host copy writes it (no separate zeroing pass)
+        py::module_ np = py::module_::import("numpy");
+        py::tuple t(shape.size());
+        for (size_t i = 0; i < shape.size(); ++i)
+            t[i] = py::int_(shape[i]);
+        py::array arr = np.attr("zeros")(t, "dtype"_a = np.attr("complex128"));
         o.keep = arr;
         o.ptr = arr.mutable_data();
     }
