@@ -482,6 +482,77 @@ int64_t family_partials(const fpg_operator *op, const ExpectPlan &plan, int64_t 
     return total;
 }
 
+// A second stream forked from st (after all of st's work so far) and joined
+// back into it: per caller stream, one non-blocking stream of the same
+// priority, created on first use and kept.  Without a fork (or when no side
+// stream can be had) stream() is st itself.
+class SideStream
+{
+  public:
+    SideStream(cudaStream_t st, bool fork) : st_(st)
+    {
+        if (!fork || !(side_ = side_for(st)))
+            return;
+        if (cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&join_, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventRecord(fork_, st) != cudaSuccess || cudaStreamWaitEvent(side_, fork_, 0) != cudaSuccess)
+        {
+            cudaGetLastError();
+            side_ = nullptr;
+        }
+    }
+    ~SideStream()
+    {
+        join();
+        if (fork_)
+            cudaEventDestroy(fork_);
+        if (join_)
+            cudaEventDestroy(join_);
+    }
+    cudaStream_t stream() const
+    {
+        return side_ ? side_ : st_;
+    }
+    // st waits for everything queued on the side stream (idempotent)
+    cudaError_t join()
+    {
+        if (!side_ || joined_)
+            return cudaSuccess;
+        joined_ = true;
+        cudaError_t e = cudaEventRecord(join_, side_);
+        if (e == cudaSuccess)
+            e = cudaStreamWaitEvent(st_, join_, 0);
+        return e;
+    }
+
+  private:
+    static cudaStream_t side_for(cudaStream_t st)
+    {
+        static std::mutex mu;
+        static std::vector<std::pair<cudaStream_t, cudaStream_t>> map;
+        std::lock_guard<std::mutex> lock(mu);
+        for (auto &kv : map)
+            if (kv.first == st)
+                return kv.second;
+        if (map.size() >= 64)
+            return nullptr;
+        int prio = 0;
+        cudaStream_t s = nullptr;
+        if (cudaStreamGetPriority(st, &prio) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return nullptr;
+        }
+        map.emplace_back(st, s);
+        return s;
+    }
+    cudaStream_t st_;
+    cudaStream_t side_ = nullptr;
+    cudaEvent_t fork_ = nullptr, join_ = nullptr;
+    bool joined_ = false;
+};
+
 // The apply stage.  float32 as is; float64 in df64 on the float32 pipes:
 // state and coefficients split once (and range-checked) into df64 copies,
 // the df64 kernel, then the float64 kernel, which returns at once unless a
@@ -558,17 +629,31 @@ int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int6
     };
     DevOp d;
     ExpectPlan pl;
+    // the transform and marginal families run on a side stream, concurrently
+    // with the pair and direct families on st: their CTAs fill the SMs that
+    // the other kernels' last waves leave idle (every family writes its own
+    // strings' rows)
+    SideStream side(st, !op->pairs.empty() && (!op->wht.empty() || !op->margs.empty()));
+    const cudaStream_t st2 = side.stream();
     if (!op->wht.empty())
     {
         double *dst = target(kFamWht, d, pl);
         FPG_CUDA(launch_expect_wht(fp32, psi, S, op->n, d, op->d_wht, (int)op->wht.size(), op->wht_max_count,
-                                   op->wht_both, pl.wht_TC, pl.wht_ctiles, pl.n_splits, dst, range_flag, psi_df, st));
+                                   op->wht_both, pl.wht_TC, pl.wht_ctiles, pl.n_splits, dst, range_flag, psi_df, st2));
+        if (off[kFamWht] >= 0)
+            FPG_CUDA(launch_reduce_family(partials + off[kFamWht], plan.fam_splits[kFamWht],
+                                          op->fam_begin[kFamWht + 1] - op->fam_begin[kFamWht], S,
+                                          op->d_glob + op->fam_begin[kFamWht], ev, st2));
     }
     if (!op->margs.empty())
     {
         double *dst = target(kFamMarg, d, pl);
         FPG_CUDA(launch_expect_marg(fp32, psi, S, op->n, d, op->d_margs, (int)op->margs.size(), op->marg_max_high,
-                                    pl.wht_TC, pl.wht_ctiles, pl.n_splits, dst, range_flag, psi_df, st));
+                                    pl.wht_TC, pl.wht_ctiles, pl.n_splits, dst, range_flag, psi_df, st2));
+        if (off[kFamMarg] >= 0)
+            FPG_CUDA(launch_reduce_family(partials + off[kFamMarg], plan.fam_splits[kFamMarg],
+                                          op->fam_begin[kFamMarg + 1] - op->fam_begin[kFamMarg], S,
+                                          op->d_glob + op->fam_begin[kFamMarg], ev, st2));
     }
     if (!op->pairs.empty())
     {
@@ -586,10 +671,11 @@ int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int6
         }
     }
     for (int f = 0; f < kNumFam; ++f)
-        if (off[f] >= 0)
+        if (off[f] >= 0 && f != kFamWht && f != kFamMarg)
             FPG_CUDA(launch_reduce_family(partials + off[f], plan.fam_splits[f],
                                           op->fam_begin[f + 1] - op->fam_begin[f], S, op->d_glob + op->fam_begin[f],
                                           ev, st));
+    FPG_CUDA(side.join());
     return FPG_OK;
 }
 
