@@ -992,16 +992,29 @@ extern "C"
             return set_error(FPG_ERR_CUDA, "cannot select the operator's device");
         cudaStream_t st = (cudaStream_t)stream;
         const bool fp32 = dtype == FPG_C64;
-        // per-string table, then (float64) the contraction's df64 range flag
+        // per-string table, then (float64) the contraction's flag
         Scratch evb(st);
         const size_t ev_bytes = ((size_t)op->P * (size_t)n_states * sizeof(double) + 255) & ~(size_t)255;
         FPG_CUDA(evb.alloc(ev_bytes + 256));
-        if (int rc = run_expect_strings(op, states, (double *)evb.p, n_states, fp32, st))
+        int *flag = (int *)((char *)evb.p + ev_bytes);
+        Scratch ws(st);
+        if (!fp32)
+        {
+            // float64: the H half of the contraction's preparation runs on a
+            // side stream while the per-string stage computes
+            FPG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+            FPG_CUDA(ws.alloc(oz_workspace_bytes(2 * n_operators, n_states, op->P)));
+            SideStream side(st, true);
+            FPG_CUDA(launch_contract_oz_prep_h(coeffs, op->P, n_operators, n_states, ws.p, flag, side.stream()));
+            if (int rc = run_expect_strings(op, states, (double *)evb.p, n_states, fp32, st))
+                return rc;
+            FPG_CUDA(side.join());
+        }
+        else if (int rc = run_expect_strings(op, states, (double *)evb.p, n_states, fp32, st))
             return rc;
         if (fp32)
         {
             // mixed path: 3xTF32 contraction on the tensor cores
-            Scratch ws(st);
             FPG_CUDA(ws.alloc(tc_workspace_bytes(2 * n_operators, n_states, op->P)));
             FPG_CUDA(launch_contract_tc_expect(coeffs, (const double *)evb.p, op->P, n_operators, n_states, out,
                                                ws.p, st));
@@ -1009,10 +1022,6 @@ extern "C"
         }
         // float64: the contraction on the tensor cores (exact digit-slice
         // products), or the float64 GEMM when H or E holds a non-finite value
-        int *flag = (int *)((char *)evb.p + ev_bytes);
-        FPG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
-        Scratch ws(st);
-        FPG_CUDA(ws.alloc(oz_workspace_bytes(2 * n_operators, n_states, op->P)));
         FPG_CUDA(launch_contract_oz_expect(coeffs, (const double *)evb.p, op->P, n_operators, n_states, out, ws.p,
                                            flag, st));
         FPG_CUDA(launch_contract_f64_if(coeffs, (const double *)evb.p, op->P, n_operators, n_states, out, flag, st));

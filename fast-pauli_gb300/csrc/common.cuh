@@ -239,7 +239,11 @@ cudaError_t launch_weighted_tc(const void *H, const float *X, int64_t P, int64_t
 // flag: device int, zero before the call; raised when H or E holds a
 // non-finite value, in which case these kernels leave out untouched and
 // launch_contract_f64_if computes the contraction.
+// The H half of its preparation (row scales and digit slices of H), which
+// may run on another stream before the rest (ordered after it by the caller).
 size_t oz_workspace_bytes(int64_t M, int64_t N, int64_t Kd);
+cudaError_t launch_contract_oz_prep_h(const void *H, int64_t P, int64_t K, int64_t S, void *ws, int *flag,
+                                      cudaStream_t st);
 cudaError_t launch_contract_oz_expect(const void *H, const double *E, int64_t P, int64_t K, int64_t S, void *out,
                                       void *ws, int *flag, cudaStream_t st);
 // The float64 CUDA-core contraction (complex128 H and out), run only when

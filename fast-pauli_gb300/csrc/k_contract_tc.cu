@@ -976,6 +976,34 @@ size_t oz_workspace_bytes(int64_t M, int64_t N, int64_t Kd)
            256;
 }
 
+namespace
+{
+int64_t oz_rows_per_block(int64_t P)
+{
+    return P > 8 * 4096 ? (P + 4095) / 4096 : 8; // grid y <= 4096
+}
+} // namespace
+
+cudaError_t launch_contract_oz_prep_h(const void *H, int64_t P, int64_t K, int64_t S, void *ws, int *flag,
+                                      cudaStream_t st)
+{
+    if (K <= 0 || S <= 0 || P <= 0)
+        return cudaSuccess;
+    const OzLayout g = oz_layout(2 * K, S, P, ws);
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(g.max_a, 0, (size_t)g.Mp * 8, st)))
+        return e;
+    const int64_t rows_per_block = oz_rows_per_block(P);
+    const unsigned py = (unsigned)((P + rows_per_block - 1) / rows_per_block);
+    k_oz_max_h<<<dim3((unsigned)((K + 127) / 128), py), 128, 0, st>>>((const double2 *)H, P, K, rows_per_block,
+                                                                      g.max_a, flag);
+    if ((e = launched()))
+        return e;
+    k_oz_slice<true><<<grid_for(g.Mp * (g.Kp / 8)), 256, 0, st>>>(H, P, K, 2 * K, g.Mp, g.Kp, OZ_TM, g.max_a, flag,
+                                                                  g.a_sl, g.exp_a);
+    return launched();
+}
+
 cudaError_t launch_contract_oz_expect(const void *H, const double *E, int64_t P, int64_t K, int64_t S, void *out,
                                       void *ws, int *flag, cudaStream_t st)
 {
@@ -983,19 +1011,11 @@ cudaError_t launch_contract_oz_expect(const void *H, const double *E, int64_t P,
         return cudaSuccess;
     const OzLayout g = oz_layout(2 * K, S, P, ws);
     cudaError_t e;
-    if ((e = cudaMemsetAsync(g.max_a, 0, (size_t)(g.Mp + g.Np) * 8, st)))
+    if ((e = cudaMemsetAsync(g.max_b, 0, (size_t)g.Np * 8, st)))
         return e;
-    const int64_t rows_per_block = P > 8 * 4096 ? (P + 4095) / 4096 : 8; // grid y <= 4096
+    const int64_t rows_per_block = oz_rows_per_block(P);
     const unsigned py = (unsigned)((P + rows_per_block - 1) / rows_per_block);
-    k_oz_max_h<<<dim3((unsigned)((K + 127) / 128), py), 128, 0, st>>>((const double2 *)H, P, K, rows_per_block,
-                                                                      g.max_a, flag);
-    if ((e = launched()))
-        return e;
     k_oz_max_e<<<dim3((unsigned)((S + 127) / 128), py), 128, 0, st>>>(E, P, S, rows_per_block, g.max_b, flag);
-    if ((e = launched()))
-        return e;
-    k_oz_slice<true><<<grid_for(g.Mp * (g.Kp / 8)), 256, 0, st>>>(H, P, K, 2 * K, g.Mp, g.Kp, OZ_TM, g.max_a, flag,
-                                                                  g.a_sl, g.exp_a);
     if ((e = launched()))
         return e;
     k_oz_slice<false><<<grid_for(g.Np * (g.Kp / 8)), 256, 0, st>>>(E, P, S, S, g.Np, g.Kp, OZ_TN, g.max_b, flag,
