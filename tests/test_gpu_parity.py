@@ -104,6 +104,28 @@ def test_weight2_strings_summed_expectation(n, S):
     assert normwise(got, oracle.summed_expectation(strings, h, psi)) < TOL_C128
 
 
+@pytest.mark.parametrize("n,S", [(22, 3), (20, 18)])
+def test_large_n_weight2_subset(n, S):
+    """Row indices past 2^20: a random subset of the weight <= 2 strings
+    (every kernel family: pair, marginal with up to 17 high row bits,
+    transform) against the oracle: expectation and apply_weighted."""
+    rng = np.random.default_rng(1000 + n)
+    every = oracle.calculate_pauli_strings_max_weight(n, 2)
+    pick = sorted(set(rng.choice(len(every), size=70, replace=False).tolist()) | {1, 2, 3})
+    strings = [every[i] for i in pick]
+    # a whole one-position group and part of the diagonal group
+    strings += [s for s in every if s.startswith("X") and s.count("I") >= n - 2][:30]
+    strings += [s for s in every if set(s) <= {"I", "Z"}][:20]
+    strings = list(dict.fromkeys(strings))
+    P, K = len(strings), 2
+    h = (rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))) / np.sqrt(2 * P)
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    sop = fp.SummedPauliOp(strings, h)
+    assert normwise(sop.expectation_value(psi), oracle.summed_expectation(strings, h, psi)) < TOL_C128
+    data = rng.standard_normal((K, S))
+    assert normwise(sop.apply_weighted(psi, data), oracle.summed_apply_weighted(strings, h, psi, data)) < TOL_C128
+
+
 @pytest.mark.parametrize("kind", ["weight2", "uniform", "weight2_c64", "weight2_tiny"])
 def test_pinned_host_states(kind):
     """Pinned host states (as torch's pinned tensors give them): float64 and
