@@ -483,9 +483,10 @@ int64_t family_partials(const fpg_operator *op, const ExpectPlan &plan, int64_t 
 }
 
 // A second stream forked from st (after all of st's work so far) and joined
-// back into it: per caller stream, one non-blocking stream of the same
-// priority, created on first use and kept.  Without a fork (or when no side
-// stream can be had) stream() is st itself.
+// back into it: per caller stream (per thread for the per-thread and legacy
+// default handles), one non-blocking stream of the same priority, created on
+// first use and kept.  Without a fork (or when no side stream can be had)
+// stream() is st itself.
 class SideStream
 {
   public:
@@ -526,16 +527,8 @@ class SideStream
     }
 
   private:
-    static cudaStream_t side_for(cudaStream_t st)
+    static cudaStream_t make_like(cudaStream_t st)
     {
-        static std::mutex mu;
-        static std::vector<std::pair<cudaStream_t, cudaStream_t>> map;
-        std::lock_guard<std::mutex> lock(mu);
-        for (auto &kv : map)
-            if (kv.first == st)
-                return kv.second;
-        if (map.size() >= 64)
-            return nullptr;
         int prio = 0;
         cudaStream_t s = nullptr;
         if (cudaStreamGetPriority(st, &prio) != cudaSuccess ||
@@ -544,7 +537,31 @@ class SideStream
             cudaGetLastError();
             return nullptr;
         }
-        map.emplace_back(st, s);
+        return s;
+    }
+    static cudaStream_t side_for(cudaStream_t st)
+    {
+        // the per-thread and legacy default handles name a different stream
+        // in every thread (or one shared by all): a side stream per thread
+        if (st == cudaStreamPerThread || st == nullptr || st == cudaStreamLegacy)
+        {
+            thread_local cudaStream_t mine[2] = {nullptr, nullptr};
+            cudaStream_t &s = mine[st == cudaStreamPerThread ? 0 : 1];
+            if (!s)
+                s = make_like(st);
+            return s;
+        }
+        static std::mutex mu;
+        static std::vector<std::pair<cudaStream_t, cudaStream_t>> map;
+        std::lock_guard<std::mutex> lock(mu);
+        for (auto &kv : map)
+            if (kv.first == st)
+                return kv.second;
+        if (map.size() >= 64)
+            return nullptr;
+        cudaStream_t s = make_like(st);
+        if (s)
+            map.emplace_back(st, s);
         return s;
     }
     cudaStream_t st_;

@@ -152,6 +152,36 @@ def test_pinned_host_states(kind):
     assert normwise(got, want) < tol
 
 
+def test_concurrent_host_calls_from_threads():
+    """Calls from several host threads at once (each on its per-thread
+    stream, each with its own side stream for the concurrent kernel
+    families) give the results of the same calls made one at a time."""
+    import threading
+
+    rng = np.random.default_rng(78)
+    n, S = 10, 40
+    strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
+    P, K = len(strings), 3
+    ops = []
+    for j in range(4):
+        h = (rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))) / np.sqrt(2 * P)
+        ops.append((fp.SummedPauliOp(strings, h), oracle.unit_norm_states(rng, 1 << n, S)))
+    alone = [op.expectation_value(psi) for op, psi in ops]
+    got = [None] * len(ops)
+
+    def run(j):
+        for _ in range(3):
+            got[j] = ops[j][0].expectation_value(ops[j][1])
+
+    threads = [threading.Thread(target=run, args=(j,)) for j in range(len(ops))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for j in range(len(ops)):
+        np.testing.assert_array_equal(got[j], alone[j])
+
+
 def test_pool_memory_reused_and_released():
     # temporaries come from the library's pool: back-to-back host-buffer
     # calls (each synchronises) reuse it; after release_cached_memory the
