@@ -849,10 +849,12 @@ template <std::floating_point T, typename H = std::complex<T>> struct PauliOp
                 sb += CD(c);
             return PauliOp(std::vector<H>{H(sa * sb)}, std::vector<PauliString>{PauliString(std::vector<Pauli>{})});
         }
+        const size_t N = Pa * Pb;
+        if (N >= (size_t(1) << 31))
+            throw std::runtime_error("fast_pauli (GPU): too many string pairs in a PauliOp product (>= 2^31)");
         fpg_operator *oa = lhs.cache_.get(lhs.pauli_strings), *ob = rhs.cache_.get(rhs.pauli_strings);
         cudaStream_t st = detail::stream();
         const std::vector<CD> ca(lhs.coeffs.begin(), lhs.coeffs.end()), cb(rhs.coeffs.begin(), rhs.coeffs.end());
-        const size_t N = Pa * Pb;
         detail::DevBuf da(Pa * sizeof(CD), st), db(Pb * sizeof(CD), st), ox(N * 8, st), oz(N * 8, st),
             oc(N * sizeof(CD), st);
         detail::cuda_check(cudaMemcpyAsync(da.p, ca.data(), da.bytes, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
