@@ -96,6 +96,21 @@ struct ArF32
     {
         const float2 a = __ldg(reinterpret_cast<const float2 *>(psi) + ea);
         const float2 b = __ldg(reinterpret_cast<const float2 *>(psi) + eb);
+        qraw(a, b, re, im, vr, vi);
+    }
+    // small elements: a block half's 32 loads are issued before any use
+    static constexpr bool kPrefetchHalf = true;
+    using raw_t = float2;
+    static __device__ __forceinline__ raw_t ld(const in_t *psi, int64_t e)
+    {
+        return __ldg(reinterpret_cast<const float2 *>(psi) + e);
+    }
+    static __device__ __forceinline__ raw_t raw_zero()
+    {
+        return make_float2(0.f, 0.f);
+    }
+    static __device__ __forceinline__ void qraw(raw_t a, raw_t b, bool re, bool im, val &vr, val &vi)
+    {
         if (re)
             vr = fmaf(a.x, b.x, a.y * b.y);
         if (im)
@@ -108,7 +123,16 @@ struct ArF32
 struct ArF64
 {
     using in_t = double;
-    static constexpr bool kRaises = false, kRecompute = true;
+    static constexpr bool kRaises = false, kRecompute = true, kPrefetchHalf = false;
+    using raw_t = double2;
+    static __device__ __forceinline__ raw_t ld(const in_t *, int64_t)
+    {
+        return make_double2(0.0, 0.0);
+    }
+    static __device__ __forceinline__ raw_t raw_zero()
+    {
+        return make_double2(0.0, 0.0);
+    }
     using val = double;
     using acc = double;
     static __device__ __forceinline__ val zero()
@@ -163,7 +187,12 @@ struct ArF64
 struct ArDF
 {
     using in_t = double;
-    static constexpr bool kRaises = true, kRecompute = false;
+    static constexpr bool kRaises = true, kRecompute = false, kPrefetchHalf = false;
+    using raw_t = float4;
+    static __device__ __forceinline__ float4 raw_zero()
+    {
+        return make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     using val = DF;
     using acc = DF;
     static __device__ __forceinline__ val zero()
@@ -256,6 +285,24 @@ __device__ __forceinline__ void block_marginals(const typename A::in_t *__restri
     for (int h = 0; h < (1 << (LB - 4)); ++h)
     {
         val hs[2] = {A::zero(), A::zero()};
+        // kPrefetchHalf: the half's 16 row pairs loaded before any use
+        typename A::raw_t ra[A::kPrefetchHalf ? 16 : 1], rb[A::kPrefetchHalf ? 16 : 1];
+        if constexpr (A::kPrefetchHalf)
+        {
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+            {
+                const uint32_t m2 = (uint32_t)(16 * h + j);
+                const uint32_t r = LB == 5 ? m2 : (((m2 >> pl) << (pl + 1)) | (m2 & ((1u << pl) - 1u)));
+                ra[j] = A::raw_zero();
+                rb[j] = A::raw_zero();
+                if ((int)r < RB)
+                {
+                    ra[j] = A::ld(psi, (int64_t)(base + r) * S + t0);
+                    rb[j] = A::ld(psi, (int64_t)(baseB + (r ^ xl)) * S + t0);
+                }
+            }
+        }
 #pragma unroll
         for (int k = 0; k < 4; ++k)
         {
@@ -263,13 +310,20 @@ __device__ __forceinline__ void block_marginals(const typename A::in_t *__restri
 #pragma unroll
             for (int u = 0; u < 4; ++u)
             {
-                const uint32_t m2 = (uint32_t)(16 * h + 4 * k + u);
-                const uint32_t r = LB == 5 ? m2 : (((m2 >> pl) << (pl + 1)) | (m2 & ((1u << pl) - 1u)));
                 v[u][0] = A::zero();
                 v[u][1] = A::zero();
-                if ((int)r < RB)
-                    A::q(psi, (int64_t)(base + r) * S + t0, (int64_t)(baseB + (r ^ xl)) * S + t0, need_re, need_im,
-                         v[u][0], v[u][1], bad);
+                if constexpr (A::kPrefetchHalf)
+                {
+                    A::qraw(ra[4 * k + u], rb[4 * k + u], need_re, need_im, v[u][0], v[u][1]);
+                }
+                else
+                {
+                    const uint32_t m2 = (uint32_t)(16 * h + 4 * k + u);
+                    const uint32_t r = LB == 5 ? m2 : (((m2 >> pl) << (pl + 1)) | (m2 & ((1u << pl) - 1u)));
+                    if ((int)r < RB)
+                        A::q(psi, (int64_t)(base + r) * S + t0, (int64_t)(baseB + (r ^ xl)) * S + t0, need_re,
+                             need_im, v[u][0], v[u][1], bad);
+                }
             }
 #pragma unroll
             for (int p = 0; p < 2; ++p)
