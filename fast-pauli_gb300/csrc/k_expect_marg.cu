@@ -99,7 +99,7 @@ struct ArF32
         qraw(a, b, re, im, vr, vi);
     }
     // small elements: a block half's 32 loads are issued before any use
-    static constexpr bool kPrefetchHalf = true;
+    static constexpr int kPrefetchRows = 16;
     using raw_t = float2;
     static __device__ __forceinline__ raw_t ld(const in_t *psi, int64_t e)
     {
@@ -123,7 +123,8 @@ struct ArF32
 struct ArF64
 {
     using in_t = double;
-    static constexpr bool kRaises = false, kRecompute = true, kPrefetchHalf = false;
+    static constexpr bool kRaises = false, kRecompute = true;
+    static constexpr int kPrefetchRows = 0;
     using raw_t = double2;
     static __device__ __forceinline__ raw_t ld(const in_t *, int64_t)
     {
@@ -187,7 +188,8 @@ struct ArF64
 struct ArDF
 {
     using in_t = double;
-    static constexpr bool kRaises = true, kRecompute = false, kPrefetchHalf = false;
+    static constexpr bool kRaises = true, kRecompute = false;
+    static constexpr int kPrefetchRows = 0;
     using raw_t = float4;
     static __device__ __forceinline__ float4 raw_zero()
     {
@@ -263,10 +265,20 @@ struct ArDFS : ArDF
 {
     using in_t = float4;
     static constexpr bool kRaises = false, kRecompute = false;
+    // 16-byte elements: loads issued four rows at a time ahead of use
+    static constexpr int kPrefetchRows = 4;
     static __device__ __forceinline__ void q(const in_t *psi, int64_t ea, int64_t eb, bool re, bool im, val &vr,
                                              val &vi, bool &)
     {
         qdf(__ldg(psi + ea), __ldg(psi + eb), re, im, vr, vi);
+    }
+    static __device__ __forceinline__ raw_t ld(const in_t *psi, int64_t e)
+    {
+        return __ldg(psi + e);
+    }
+    static __device__ __forceinline__ void qraw(raw_t a, raw_t b, bool re, bool im, val &vr, val &vi)
+    {
+        qdf(a, b, re, im, vr, vi);
     }
 };
 
@@ -285,36 +297,41 @@ __device__ __forceinline__ void block_marginals(const typename A::in_t *__restri
     for (int h = 0; h < (1 << (LB - 4)); ++h)
     {
         val hs[2] = {A::zero(), A::zero()};
-        // kPrefetchHalf: the half's 16 row pairs loaded before any use
-        typename A::raw_t ra[A::kPrefetchHalf ? 16 : 1], rb[A::kPrefetchHalf ? 16 : 1];
-        if constexpr (A::kPrefetchHalf)
-        {
-#pragma unroll
-            for (int j = 0; j < 16; ++j)
-            {
-                const uint32_t m2 = (uint32_t)(16 * h + j);
-                const uint32_t r = LB == 5 ? m2 : (((m2 >> pl) << (pl + 1)) | (m2 & ((1u << pl) - 1u)));
-                ra[j] = A::raw_zero();
-                rb[j] = A::raw_zero();
-                if ((int)r < RB)
-                {
-                    ra[j] = A::ld(psi, (int64_t)(base + r) * S + t0);
-                    rb[j] = A::ld(psi, (int64_t)(baseB + (r ^ xl)) * S + t0);
-                }
-            }
-        }
+        // kPrefetchRows > 0: the loads of that many row pairs are issued
+        // before any of them is used (batches of the half's 16)
+        constexpr int PF = A::kPrefetchRows > 0 ? A::kPrefetchRows : 1;
+        typename A::raw_t ra[PF], rb[PF];
 #pragma unroll
         for (int k = 0; k < 4; ++k)
         {
+            if constexpr (A::kPrefetchRows > 0)
+            {
+                if ((4 * k) % PF == 0)
+                {
+#pragma unroll
+                    for (int j = 0; j < PF; ++j)
+                    {
+                        const uint32_t m2 = (uint32_t)(16 * h + 4 * k + j);
+                        const uint32_t r = LB == 5 ? m2 : (((m2 >> pl) << (pl + 1)) | (m2 & ((1u << pl) - 1u)));
+                        ra[j] = A::raw_zero();
+                        rb[j] = A::raw_zero();
+                        if ((int)r < RB)
+                        {
+                            ra[j] = A::ld(psi, (int64_t)(base + r) * S + t0);
+                            rb[j] = A::ld(psi, (int64_t)(baseB + (r ^ xl)) * S + t0);
+                        }
+                    }
+                }
+            }
             val v[4][2];
 #pragma unroll
             for (int u = 0; u < 4; ++u)
             {
                 v[u][0] = A::zero();
                 v[u][1] = A::zero();
-                if constexpr (A::kPrefetchHalf)
+                if constexpr (A::kPrefetchRows > 0)
                 {
-                    A::qraw(ra[4 * k + u], rb[4 * k + u], need_re, need_im, v[u][0], v[u][1]);
+                    A::qraw(ra[(4 * k + u) % PF], rb[(4 * k + u) % PF], need_re, need_im, v[u][0], v[u][1]);
                 }
                 else
                 {
