@@ -57,7 +57,10 @@ struct W32
     static __device__ __forceinline__ void q(const in_t *psi, int64_t ea, int64_t eb, bool re, bool im, val &vr,
                                              val &vi)
     {
-        const float2 a = __ldg(psi + ea), b = __ldg(psi + eb);
+        qv(__ldg(psi + ea), __ldg(psi + eb), re, im, vr, vi);
+    }
+    static __device__ __forceinline__ void qv(in_t a, in_t b, bool re, bool im, val &vr, val &vi)
+    {
         if (re)
             vr = fmaf(a.x, b.x, a.y * b.y);
         if (im)
@@ -109,7 +112,10 @@ struct W64
     static __device__ __forceinline__ void q(const in_t *psi, int64_t ea, int64_t eb, bool re, bool im, val &vr,
                                              val &vi)
     {
-        const double2 a = __ldg(psi + ea), b = __ldg(psi + eb);
+        qv(__ldg(psi + ea), __ldg(psi + eb), re, im, vr, vi);
+    }
+    static __device__ __forceinline__ void qv(in_t a, in_t b, bool re, bool im, val &vr, val &vi)
+    {
         if (re)
             vr = fma(a.x, b.x, a.y * b.y);
         if (im)
@@ -158,7 +164,10 @@ struct WDF
     static __device__ __forceinline__ void q(const in_t *psi, int64_t ea, int64_t eb, bool re, bool im, val &vr,
                                              val &vi)
     {
-        const float4 a = __ldg(psi + ea), b = __ldg(psi + eb);
+        qv(__ldg(psi + ea), __ldg(psi + eb), re, im, vr, vi);
+    }
+    static __device__ __forceinline__ void qv(in_t a, in_t b, bool re, bool im, val &vr, val &vi)
+    {
         if (re)
         {
             vr = DFv{0.f, 0.f};
@@ -212,12 +221,37 @@ template <typename W> __device__ __forceinline__ void wht16(typename W::val (&v)
                 W::butterfly(v[r], v[r | s]);
 }
 
+// q of the block's 16 rows into vr / vi (one array when !BOTH: each row's
+// single part), the loads of four rows issued before any of them is used
+template <typename W, bool BOTH>
+__device__ __forceinline__ void rows_q(const typename W::in_t *__restrict__ psi, int64_t S, int64_t t0, uint64_t base,
+                                       uint64_t baseB, uint32_t xl, int RB, bool need_re, bool need_im,
+                                       typename W::val (&vr)[16], typename W::val (&vi)[16])
+{
+#pragma unroll
+    for (int r0 = 0; r0 < 16; r0 += 4)
+    {
+        typename W::in_t a[4], b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (r0 + u < RB)
+            {
+                a[u] = __ldg(psi + (int64_t)(base + r0 + u) * S + t0);
+                b[u] = __ldg(psi + (int64_t)(baseB + (uint64_t)((r0 + u) ^ xl)) * S + t0);
+            }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (r0 + u < RB)
+                W::qv(a[u], b[u], need_re, need_im, vr[r0 + u], vi[r0 + u]);
+    }
+}
+
 // only_if: when not null, the float64 recomputation returns at once unless
 // *only_if is set.
 // BOTH: some chunk of the launch has strings of both #Y parities (two
 // transforms per block); otherwise one.
 template <typename W, int SLOTS, bool BOTH>
-__global__ void __launch_bounds__(kWhtThreads)
+__global__ void __launch_bounds__(kWhtThreads, BOTH ? 1 : 2)
     k_expect_wht(const typename W::in_t *__restrict__ psi, int64_t S, int n, const StringRec *__restrict__ recs,
                  const int32_t *__restrict__ orig, int64_t P, const WhtChunk *__restrict__ chunks, int TC,
                  int n_splits, double *__restrict__ out, const int *__restrict__ only_if)
@@ -289,11 +323,7 @@ __global__ void __launch_bounds__(kWhtThreads)
                 vim[r] = W::zero();
             }
             if (have && col_ok)
-#pragma unroll
-                for (int r = 0; r < 16; ++r)
-                    if (r < RB)
-                        W::q(psi, (int64_t)(base + r) * S + t0, (int64_t)(baseB + (uint64_t)(r ^ xl)) * S + t0, need_re,
-                             need_im, vre[r], vim[r]);
+                rows_q<W, true>(psi, S, t0, base, baseB, xl, RB, need_re, need_im, vre, vim);
             if (need_re)
                 wht16<W>(vre);
             if (need_im)
@@ -315,11 +345,7 @@ __global__ void __launch_bounds__(kWhtThreads)
             for (int r = 0; r < 16; ++r)
                 v[r] = W::zero();
             if (have && col_ok)
-#pragma unroll
-                for (int r = 0; r < 16; ++r)
-                    if (r < RB)
-                        W::q(psi, (int64_t)(base + r) * S + t0, (int64_t)(baseB + (uint64_t)(r ^ xl)) * S + t0, need_re,
-                             need_im, v[r], v[r]);
+                rows_q<W, false>(psi, S, t0, base, baseB, xl, RB, need_re, need_im, v, v);
             wht16<W>(v);
             cell *w = need_re ? w0 : w1;
 #pragma unroll
