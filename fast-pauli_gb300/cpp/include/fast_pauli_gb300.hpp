@@ -21,6 +21,7 @@
 #include <array>
 #include <complex>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <execution>
 #include <functional>
@@ -245,6 +246,73 @@ struct StreamScope
 inline void sync(cudaStream_t st)
 {
     cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+}
+
+// Page-locked host memory (cudaHostAlloc / cudaHostRegister): copies from it
+// are asynchronous, so they can overlap computation.
+inline bool pinned_host(const void *p)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+// The calling thread's stream for host-to-device copies that overlap the
+// computation on the call's stream (created on first use).
+inline cudaStream_t copy_stream()
+{
+    struct Holder
+    {
+        cudaStream_t s = nullptr;
+        ~Holder()
+        {
+            if (s)
+                cudaStreamDestroy(s);
+        }
+    };
+    static thread_local Holder h;
+    if (!h.s)
+        cuda_check(cudaStreamCreateWithFlags(&h.s, cudaStreamNonBlocking), "cudaStreamCreateWithFlags");
+    return h.s;
+}
+
+struct Event
+{
+    cudaEvent_t e = nullptr;
+    Event()
+    {
+        cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreateWithFlags");
+    }
+    Event(const Event &) = delete;
+    Event &operator=(const Event &) = delete;
+    ~Event()
+    {
+        cudaEventDestroy(e);
+    }
+};
+
+// Column chunks of a call whose states are `bytes` of pinned host memory in
+// S columns: chunk c + 1 is copied in while chunk c is computed (columns are
+// independent).  Two by default (a narrower call costs a little more per
+// column, so more chunks hide less than they add); one (no overlap) below
+// 64 MiB or 256 columns; the environment variable FPG_HOST_CHUNKS overrides
+// the count.
+inline size_t host_column_chunks(size_t S, size_t bytes)
+{
+    const size_t most = std::max<size_t>(1, S / 64);
+    if (const char *e = std::getenv("FPG_HOST_CHUNKS"))
+    {
+        const long v = std::strtol(e, nullptr, 10);
+        if (v >= 1)
+            return std::min<size_t>((size_t)v, most);
+    }
+    if (bytes < (size_t(64) << 20) || S < 256)
+        return 1;
+    return std::min<size_t>(2, most);
 }
 
 // Host-visible results must be complete before returning; device-resident
@@ -1225,8 +1293,11 @@ template <std::floating_point T> struct SummedPauliOp
             return;
         fpg_operator *op = cache_.get(pauli_strings);
         cudaStream_t st = detail::stream();
-        detail::Staged in(psi, dim() * S * sizeof(C), 0, st),
-            o(out, n_operators() * S * sizeof(C), out_zero ? 2 : 1, st);
+        const size_t in_bytes = dim() * S * sizeof(C);
+        if (!detail::on_device(out) && detail::pinned_host(psi))
+            if (const size_t nc = detail::host_column_chunks(S, in_bytes); nc > 1)
+                return run_expect_overlapped(op, out, psi, S, out_zero, nc, st);
+        detail::Staged in(psi, in_bytes, 0, st), o(out, n_operators() * S * sizeof(C), out_zero ? 2 : 1, st);
         detail::DevBuf dh = upload_coeffs<C>(st);
         detail::check(fpg_summed_expect(op, dh.p, (int64_t)n_operators(), in.dev(), o.dev(), (int64_t)S,
                                         detail::dtype_of<C>(), st));
@@ -1236,6 +1307,87 @@ template <std::floating_point T> struct SummedPauliOp
 
   private:
     detail::EncodedCache cache_;
+
+    // Pinned host states in nc column chunks: every chunk's copy is queued at
+    // once on the thread's copy stream (the link runs them back to back), each
+    // chunk is computed on the call's stream as soon as its copy has landed,
+    // and the results are copied out after the last chunk.  Each chunk is an
+    // independent fpg_summed_expect call on its own columns.
+    template <typename C>
+    void run_expect_overlapped(fpg_operator *op, C *out, const C *psi, size_t S, bool out_zero, size_t nc,
+                               cudaStream_t st) const
+    {
+        const size_t D = dim(), K = n_operators(), el = sizeof(C);
+        // widths in multiples of 64 columns: the first about a quarter of S
+        // (its computation then takes about as long as the copy of the rest,
+        // a narrower call costing a little more per column), the rest split
+        // evenly, the remainder in the last chunk
+        std::vector<size_t> c0, cw;
+        size_t left = S;
+        for (size_t c = 0; c < nc && left; ++c)
+        {
+            size_t w = c == 0 ? std::max<size_t>(64, S / 4 / 64 * 64)
+                              : std::max<size_t>(64, left / (nc - c) / 64 * 64);
+            w = c + 1 == nc ? left : std::min(w, left);
+            c0.push_back(S - left);
+            cw.push_back(w);
+            left -= w;
+        }
+        cw.back() += left;
+        nc = cw.size();
+        detail::DevBuf dh = upload_coeffs<C>(st);
+        std::vector<detail::DevBuf> din, dout;
+        din.reserve(nc);
+        dout.reserve(nc);
+        for (size_t c = 0; c < nc; ++c)
+        {
+            din.emplace_back(D * cw[c] * el, st);
+            dout.emplace_back(K * cw[c] * el, st);
+        }
+        cudaStream_t cs = detail::copy_stream();
+        detail::Event fork;
+        std::vector<std::unique_ptr<detail::Event>> landed(nc);
+        // whatever happens below, the call's stream waits for every queued
+        // copy before the buffers go back to the pool on that stream
+        struct JoinCopies
+        {
+            std::vector<std::unique_ptr<detail::Event>> &ev;
+            cudaStream_t st;
+            ~JoinCopies()
+            {
+                for (auto &e : ev)
+                    if (e)
+                        cudaStreamWaitEvent(st, e->e, 0);
+            }
+        } join{landed, st};
+        detail::cuda_check(cudaEventRecord(fork.e, st), "cudaEventRecord");
+        detail::cuda_check(cudaStreamWaitEvent(cs, fork.e, 0), "cudaStreamWaitEvent");
+        for (size_t c = 0; c < nc; ++c)
+        {
+            detail::cuda_check(cudaMemcpy2DAsync(din[c].p, cw[c] * el, psi + c0[c], S * el, cw[c] * el, D,
+                                                 cudaMemcpyHostToDevice, cs),
+                               "cudaMemcpy2DAsync");
+            landed[c] = std::make_unique<detail::Event>();
+            detail::cuda_check(cudaEventRecord(landed[c]->e, cs), "cudaEventRecord");
+        }
+        for (size_t c = 0; c < nc; ++c)
+        {
+            if (out_zero)
+                detail::cuda_check(cudaMemsetAsync(dout[c].p, 0, dout[c].bytes, st), "cudaMemsetAsync");
+            else
+                detail::cuda_check(cudaMemcpy2DAsync(dout[c].p, cw[c] * el, out + c0[c], S * el, cw[c] * el, K,
+                                                     cudaMemcpyHostToDevice, st),
+                                   "cudaMemcpy2DAsync");
+            detail::cuda_check(cudaStreamWaitEvent(st, landed[c]->e, 0), "cudaStreamWaitEvent");
+            detail::check(fpg_summed_expect(op, dh.p, (int64_t)K, din[c].p, dout[c].p, (int64_t)cw[c],
+                                            detail::dtype_of<C>(), st));
+        }
+        for (size_t c = 0; c < nc; ++c)
+            detail::cuda_check(cudaMemcpy2DAsync(out + c0[c], S * el, dout[c].p, cw[c] * el, cw[c] * el, K,
+                                                 cudaMemcpyDeviceToHost, st),
+                               "cudaMemcpy2DAsync");
+        detail::sync(st);
+    }
 
     static void check_ctor_inputs(std::vector<PauliString> const &ps, size_t rows)
     {

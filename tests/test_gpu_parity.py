@@ -152,6 +152,33 @@ def test_pinned_host_states(kind):
     assert normwise(got, want) < tol
 
 
+@pytest.mark.parametrize("chunks,S,c64", [(2, 128, False), (3, 300, False), (4, 257, True), (9, 200, False)])
+def test_pinned_host_states_in_column_chunks(monkeypatch, chunks, S, c64):
+    """Pinned host states of many columns are computed in column chunks, each
+    chunk's copy overlapping the previous chunk's computation: the results
+    (odd widths, more chunks asked for than 64-column pieces exist) match the
+    oracle and the one-call device path."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(chunks * 1000 + S)
+    n, K = 8, 5
+    strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
+    P = len(strings)
+    h = (rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))) / np.sqrt(2 * P)
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    want = oracle.summed_expectation(strings, h, psi)
+    dt = torch.complex64 if c64 else torch.complex128
+    t = torch.empty(psi.shape, dtype=dt, pin_memory=True)
+    t.copy_(torch.from_numpy(psi))
+    sop = fp.SummedPauliOp(strings, h)
+    whole = sop.expectation_value(t.cuda()).cpu().numpy()
+    monkeypatch.setenv("FPG_HOST_CHUNKS", str(chunks))
+    got = sop.expectation_value(t.numpy())
+    assert got.shape == (K, S)
+    tol = TOL_MIXED if c64 else TOL_C128
+    assert normwise(got, want) < tol
+    assert normwise(got, whole) < tol
+
+
 def test_concurrent_host_calls_from_threads():
     """Calls from several host threads at once (each on its per-thread
     stream, each with its own side stream for the concurrent kernel
