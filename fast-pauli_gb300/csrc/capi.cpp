@@ -198,6 +198,10 @@ void free_dev(fpg_operator *op)
     cudaFree(op->d_wht);
     cudaFree(op->d_pairs);
     op->d_pairs = nullptr;
+    cudaFree(op->d_tiles);
+    op->d_tiles = nullptr;
+    cudaFree(op->d_tile_pairs);
+    op->d_tile_pairs = nullptr;
     cudaFree(op->d_margs);
     op->d_margs = nullptr;
     cudaFree(op->d_local);
@@ -212,6 +216,97 @@ void free_dev(fpg_operator *op)
     op->d_wht = nullptr;
 }
 
+// The tile family: pair-kernel groups x = 2^a + 2^b (a < b) whose z' lie in
+// {0, 2^a}, gathered into units of four row bits Q with up to six groups
+// whose both bits lie in Q (k_expect_tile.cu).  Greedy cover: the first
+// group left opens a unit; its other two bits are the ones that bring the
+// most groups left into it.  Taken groups leave op->pairs for op->tiles /
+// op->tile_pairs and is_wht 4.  Operators on fewer than kTileMinQubits
+// qubits, or with fewer than kTileMinGroups such groups, keep the pair kernel.
+constexpr int kTileMinQubits = 8;
+constexpr int kTileMinGroups = 6;
+
+void build_tiles(fpg_operator *op, const std::vector<size_t> &pair_groups, std::vector<char> &is_wht)
+{
+    const int n = op->n;
+    if (n < kTileMinQubits || n > 63)
+        return;
+    // at[a * n + b]: the eligible group on bits a < b, or -1
+    std::vector<int64_t> at((size_t)n * (size_t)n, -1);
+    std::vector<int> abit_of(op->groups.size(), -1);
+    int left = 0;
+    for (size_t k = 0; k < pair_groups.size(); ++k)
+    {
+        const PairChunk &pc = op->pairs[k];
+        if (__builtin_popcountll(pc.x) != 2)
+            continue;
+        const int a = __builtin_ctzll(pc.x), b = 63 - __builtin_clzll(pc.x);
+        if (pc.abit != -1 && pc.abit != a)
+            continue;
+        at[(size_t)a * n + b] = (int64_t)pair_groups[k];
+        abit_of[pair_groups[k]] = pc.abit;
+        ++left;
+    }
+    if (left < kTileMinGroups)
+        return;
+    static const int si[kTileSlots] = {0, 0, 1, 0, 1, 2};
+    static const int sj[kTileSlots] = {1, 2, 2, 3, 3, 3};
+    auto cell = [&](int x, int y) -> int64_t & { return x < y ? at[(size_t)x * n + y] : at[(size_t)y * n + x]; };
+    size_t scan = 0;
+    while (left > 0)
+    {
+        while (at[scan] < 0)
+            ++scan;
+        const int a = (int)(scan / (size_t)n), b = (int)(scan % (size_t)n);
+        int best = -1, bc = -1, bd = -1;
+        for (int c = 0; c < n; ++c)
+        {
+            if (c == a || c == b)
+                continue;
+            for (int d = c + 1; d < n; ++d)
+            {
+                if (d == a || d == b)
+                    continue;
+                const int q[4] = {a, b, c, d};
+                int cnt = 0;
+                for (int i = 0; i < 4; ++i)
+                    for (int j = i + 1; j < 4; ++j)
+                        cnt += cell(q[i], q[j]) >= 0;
+                if (cnt > best)
+                {
+                    best = cnt;
+                    bc = c;
+                    bd = d;
+                }
+            }
+        }
+        int q[4] = {a, b, bc, bd};
+        std::sort(q, q + 4);
+        TileChunk t{};
+        for (int k = 0; k < 4; ++k)
+            t.q[k] = (int8_t)q[k];
+        for (int s = 0; s < kTileSlots; ++s)
+        {
+            int64_t &g = cell(q[si[s]], q[sj[s]]);
+            if (g < 0)
+                continue;
+            const Group &grp = op->groups[(size_t)g];
+            t.begin[s] = grp.begin;
+            t.count[s] = (int8_t)grp.count;
+            op->tile_pairs.push_back(PairChunk{grp.x, grp.begin, grp.count, abit_of[(size_t)g], 0});
+            is_wht[(size_t)g] = 4;
+            g = -1;
+            --left;
+        }
+        op->tiles.push_back(t);
+    }
+    std::vector<PairChunk> rest;
+    for (size_t k = 0; k < pair_groups.size(); ++k)
+        if (is_wht[pair_groups[k]] == 2)
+            rest.push_back(op->pairs[k]);
+    op->pairs.swap(rest);
+}
+
 // Per-call decomposition of the x-groups, by the signs z' (z with the pairing
 // bit dropped) of their strings:
 //   all z' in {0, e_a}, <= kPairMaxStrings strings   -> pair kernel;
@@ -224,10 +319,13 @@ void build_fast_decomposition(fpg_operator *op)
     op->wht_max_count = 0;
     op->wht_both = false;
     op->pairs.clear();
+    op->tiles.clear();
+    op->tile_pairs.clear();
     op->margs.clear();
     op->marg_max_high = 0;
     std::vector<std::vector<Chunk>> by_class(kNumChunkClasses);
-    std::vector<char> is_wht(op->groups.size(), 0); // 1: transform, 2: pair, 3: marginal kernel
+    std::vector<char> is_wht(op->groups.size(), 0); // 1: transform, 2: pair, 3: marginal, 4: tile kernel
+    std::vector<size_t> pair_groups;
     for (size_t gi = 0; gi < op->groups.size(); ++gi)
     {
         const Group &g = op->groups[gi];
@@ -248,6 +346,7 @@ void build_fast_decomposition(fpg_operator *op)
             // pair kernel: every z' in {0, e_a}
             is_wht[gi] = 2;
             op->pairs.push_back(PairChunk{g.x, g.begin, g.count, bits ? __builtin_ctzll(bits) : -1, 0});
+            pair_groups.push_back(gi);
             continue;
         }
         const int high = __builtin_popcountll(bits & ~31ull);
@@ -274,6 +373,7 @@ void build_fast_decomposition(fpg_operator *op)
             op->wht_both = op->wht_both || (ne > 0 && ne < cnt);
         }
     }
+    build_tiles(op, pair_groups, is_wht);
     // direct chunks of the remaining groups, in the order of the full decomposition
     for (int c = 0; c < kNumChunkClasses; ++c)
         for (int i = op->class_begin[(size_t)c]; i < op->class_begin[(size_t)c + 1]; ++i)
@@ -297,7 +397,7 @@ void build_fast_decomposition(fpg_operator *op)
     op->fast_class_begin[kNumChunkClasses] = (int)op->fast_chunks.size();
 
     // family-local string order (each family may write its own partial table)
-    static const int fam_of[4] = {kFamDirect, kFamWht, kFamPair, kFamMarg}; // by is_wht value
+    static const int fam_of[5] = {kFamDirect, kFamWht, kFamPair, kFamMarg, kFamTile}; // by is_wht value
     op->local.assign((size_t)op->P, 0);
     op->glob.clear();
     op->glob.reserve((size_t)op->P);
@@ -458,6 +558,16 @@ ExpectPlan plan_expect(const fpg_operator *op, int64_t S, bool fp32, const void 
         pick((int64_t)op->margs.size() * p.wht_ctiles, NB / 2, 256 / p.wht_TC, over1, kWindowBlocks);
     p.fam_splits[kFamWht] =
         pick((int64_t)op->wht.size() * p.wht_ctiles, NB16 / 2, kWhtThreads / p.wht_TC, over1, 2 * kWindowBlocks);
+    // the tile kernel: one element per lane (the V = 1 tiling), its column
+    // tile within the L2 budget (its units read rows spread over the whole
+    // state), the df64 copy of the state for the float64 path
+    p.tile_kernel = !op->tiles.empty() && !over1 && op->n >= 4 &&
+                    (fp32 || ((int64_t)1 << op->n) * S * 16 <= kDfSplitMaxBytes);
+    p.tile_TC = p.wht_TC;
+    p.tile_ctiles = p.wht_ctiles;
+    p.fam_splits[kFamTile] =
+        p.tile_kernel ? pick((int64_t)op->tiles.size() * p.tile_ctiles, NB16, 256 / p.tile_TC, false, 0)
+                      : pick((int64_t)op->tile_pairs.size() * p.n_ctiles, NB / 2, 256 / p.TC, over, kWindowBlocks);
     p.n_splits = 1;
     for (int f = 0; f < kNumFam; ++f)
         p.n_splits = std::max(p.n_splits, p.fam_splits[f]);
@@ -614,7 +724,8 @@ int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int6
     const int64_t scratch = family_partials(op, plan, S, off);
     // scratch: the df64 range flag of the float64 path (see df64.cuh) and the
     // families' partial tables
-    const bool need_flag = !fp32 && (!op->pairs.empty() || !op->margs.empty() || !op->wht.empty());
+    const bool need_flag =
+        !fp32 && (!op->pairs.empty() || !op->tiles.empty() || !op->margs.empty() || !op->wht.empty());
     const size_t flag_bytes = need_flag ? 256 : 0;
     Scratch partial(st);
     if (scratch > 0 || need_flag)
@@ -650,7 +761,7 @@ int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int6
     // with the pair and direct families on st: their CTAs fill the SMs that
     // the other kernels' last waves leave idle (every family writes its own
     // strings' rows)
-    SideStream side(st, !op->pairs.empty() && (!op->wht.empty() || !op->margs.empty()));
+    SideStream side(st, (!op->pairs.empty() || !op->tiles.empty()) && (!op->wht.empty() || !op->margs.empty()));
     const cudaStream_t st2 = side.stream();
     if (!op->wht.empty())
     {
@@ -671,6 +782,21 @@ int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int6
             FPG_CUDA(launch_reduce_family(partials + off[kFamMarg], plan.fam_splits[kFamMarg],
                                           op->fam_begin[kFamMarg + 1] - op->fam_begin[kFamMarg], S,
                                           op->d_glob + op->fam_begin[kFamMarg], ev, st2));
+    }
+    if (!op->tiles.empty())
+    {
+        double *dst = target(kFamTile, d, pl);
+        if (plan.tile_kernel)
+        {
+            FPG_CUDA(launch_expect_tile(fp32, fp32 ? psi : psi_df, S, op->n, d, op->d_tiles, (int)op->tiles.size(),
+                                        plan.tile_TC, plan.tile_ctiles, pl.n_splits, dst, st));
+            if (!fp32)
+                FPG_CUDA(launch_expect_pair_f64_if(psi, S, op->n, d, op->d_tile_pairs, (int)op->tile_pairs.size(), pl,
+                                                   dst, range_flag, st));
+        }
+        else
+            FPG_CUDA(launch_expect_pair(fp32, psi, S, op->n, d, op->d_tile_pairs, (int)op->tile_pairs.size(), pl, dst,
+                                        range_flag, psi_df, st));
     }
     if (!op->pairs.empty())
     {
@@ -717,7 +843,8 @@ size_t request_scratch_bytes(const fpg_operator *op, int64_t K, int64_t S, bool 
     int64_t off[kNumFam];
     size_t b = P * (size_t)S * sizeof(double) + (size_t)family_partials(op, plan, S, off) * sizeof(double) + 512;
     const int64_t split_bytes = ((int64_t)1 << op->n) * S * 16;
-    if (!fp32 && (!op->pairs.empty() || !op->margs.empty() || !op->wht.empty()) && split_bytes <= kDfSplitMaxBytes)
+    if (!fp32 && (!op->pairs.empty() || !op->tiles.empty() || !op->margs.empty() || !op->wht.empty()) &&
+        split_bytes <= kDfSplitMaxBytes)
         b += (size_t)split_bytes; // the df64 copy of the state
     b += fp32 ? tc_workspace_bytes(2 * K, S, op->P) : oz_workspace_bytes(2 * K, S, op->P);
     return b + 4096;
@@ -863,6 +990,10 @@ extern "C"
         if (e == cudaSuccess)
             e = upload(&op->d_pairs, op->pairs);
         if (e == cudaSuccess)
+            e = upload(&op->d_tiles, op->tiles);
+        if (e == cudaSuccess)
+            e = upload(&op->d_tile_pairs, op->tile_pairs);
+        if (e == cudaSuccess)
             e = upload(&op->d_margs, op->margs);
         if (e == cudaSuccess)
             e = upload(&op->d_local, op->local);
@@ -927,7 +1058,9 @@ extern "C"
             // 16-point transform: 4 adds per row per part; one add per string per 16 rows
             adds += rows * 4 * parts + (rows / 16) * w.count;
         }
-        for (const PairChunk &pc : op->pairs)
+        std::vector<PairChunk> all_pairs(op->pairs);
+        all_pairs.insert(all_pairs.end(), op->tile_pairs.begin(), op->tile_pairs.end());
+        for (const PairChunk &pc : all_pairs)
         {
             const bool paired = pc.x != 0; // rows paired across or inside 32-row blocks
             const int64_t rows = paired ? D / 2 : D;
@@ -941,7 +1074,8 @@ extern "C"
             adds += rows * parts * 17 / 8; // marginal tree: 68 adds per 32 rows and part
         }
         if (n_chunks)
-            *n_chunks = (int64_t)(op->fast_chunks.size() + op->wht.size() + op->pairs.size() + op->margs.size());
+            *n_chunks = (int64_t)(op->fast_chunks.size() + op->wht.size() + op->pairs.size() + op->tiles.size() +
+                                  op->margs.size());
         if (row_visits)
             *row_visits = visits;
         if (sign_adds)

@@ -78,6 +78,20 @@ struct PairChunk
 };
 constexpr int kPairMaxStrings = 16;
 
+// Work unit of the tile kernel (k_expect_tile.cu): four row bits
+// q[0] < q[1] < q[2] < q[3] and up to kTileSlots two-position x-groups
+// x = 2^q[i] + 2^q[j], slot s <-> (i, j) = (0,1) (0,2) (1,2) (0,3) (1,3) (2,3),
+// whose strings [begin[s], begin[s] + count[s]) all have z' in {0, 2^q[i]}
+// (count 0: empty slot).
+constexpr int kTileSlots = 6;
+struct TileChunk
+{
+    int32_t begin[kTileSlots];
+    int8_t count[kTileSlots];
+    int8_t q[4];
+    int8_t pad[6];
+};
+
 // Work unit of the marginal kernel (k_expect_marg.cu): a whole x-group
 // [begin, begin + count) whose strings each have z' (z without the pairing
 // bit) of at most one bit; zmask = the union of the z', of which at most
@@ -156,7 +170,8 @@ enum
     kFamPair = 1,
     kFamMarg = 2,
     kFamWht = 3,
-    kNumFam = 4
+    kFamTile = 4,
+    kNumFam = 5
 };
 
 struct ExpectPlan
@@ -168,6 +183,9 @@ struct ExpectPlan
     int wht_TC;       // column lanes of the V = 1 kernels (transform, marginal)
     int wht_ctiles;   // their column tiles
     int fam_splits[kNumFam]; // per-call path: row splits of each family
+    bool tile_kernel; // the tile family runs the tile kernel (else the pair kernel)
+    int tile_TC;      // its column lanes (one element each) and column tiles
+    int tile_ctiles;
 };
 
 // ev_or_partial: [n_splits][P][S] float64 (row-major), string index orig[s].
@@ -191,6 +209,18 @@ cudaError_t launch_reduce_family(const double *partial, int n_splits, int64_t Pf
 cudaError_t launch_expect_pair(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const PairChunk *d_chunks,
                                int n_chunks, const ExpectPlan &plan, double *out, int *range_flag,
                                const void *psi_df, cudaStream_t st);
+
+// Tile kernel over tile units (one complex element per lane, TC column lanes,
+// n_ctiles column tiles, 256 threads, n_splits row splits of the 2^(n-4)
+// tiles); writes like the pair kernel.  float64: psi = the df64 split copy of
+// the state (launch_df_split); values outside the df64 range are left to the
+// pair kernel's float64 form (launch_expect_pair_f64_if).  n >= 4.
+cudaError_t launch_expect_tile(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const TileChunk *d_units,
+                               int n_units, int TC, int n_ctiles, int n_splits, double *out, cudaStream_t st);
+// The pair kernel's float64 form alone: returns at once unless *range_flag.
+cudaError_t launch_expect_pair_f64_if(const void *psi, int64_t S, int n, const DevOp &op, const PairChunk *d_chunks,
+                                      int n_chunks, const ExpectPlan &plan, double *out, const int *range_flag,
+                                      cudaStream_t st);
 
 // Marginal kernel over marginal chunks: one complex element per lane, TC
 // column lanes (the V = 1 tiling, plan.wht_TC / wht_ctiles), 256 threads;

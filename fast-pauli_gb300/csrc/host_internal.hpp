@@ -52,6 +52,13 @@ struct fpg_operator
     bool wht_both = false; // some transform chunk has strings of both #Y parities
     std::vector<fpg::PairChunk> pairs; // groups served by the pair kernel
     fpg::PairChunk *d_pairs = nullptr;
+    // two-position groups served by the tile kernel, and the same groups as
+    // pair chunks (for the pair kernel when a call cannot use the tile
+    // kernel, and for the float64 recomputation)
+    std::vector<fpg::TileChunk> tiles;
+    fpg::TileChunk *d_tiles = nullptr;
+    std::vector<fpg::PairChunk> tile_pairs;
+    fpg::PairChunk *d_tile_pairs = nullptr;
     std::vector<fpg::MargChunk> margs; // groups served by the marginal kernel
     int marg_max_high = 0;
     fpg::MargChunk *d_margs = nullptr;

@@ -503,4 +503,16 @@ cudaError_t launch_expect_pair(bool fp32, const void *psi, int64_t S, int n, con
     return launched();
 }
 
+cudaError_t launch_expect_pair_f64_if(const void *psi, int64_t S, int n, const DevOp &op, const PairChunk *d_chunks,
+                                      int n_chunks, const ExpectPlan &plan, double *out, const int *range_flag,
+                                      cudaStream_t st)
+{
+    if (n_chunks <= 0)
+        return cudaSuccess;
+    dim3 grid((unsigned)n_chunks, (unsigned)plan.n_splits, (unsigned)plan.n_ctiles);
+    k_expect_pair<double, 1><<<grid, 256, 256 * sizeof(double), st>>>(
+        (const double *)psi, S, n, op.recs, op.orig, op.P, d_chunks, plan.TC, plan.n_splits, out, range_flag);
+    return launched();
+}
+
 } // namespace fpg

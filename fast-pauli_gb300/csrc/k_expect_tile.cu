@@ -1,0 +1,313 @@
+// k_expect_tile.cu -- per-string expectation values of the two-position
+// x-groups, several groups per pass over the state.
+//
+// Same quantity as k_expect_pair.cu (the per-string stage of
+// SummedPauliOp::expectation_value, fast_pauli/cpp/include/__summed_pauli_op.hpp:572-577)
+// for the groups x = e_a + e_b (a < b) whose strings all have z' (z without
+// bit b) in {0, e_a}: XX, XY, YX, YY on qubits a, b.  Each string is
+// f (U_0 +- U_1) with U_c = sum over rows r with bit b clear and bit a = c of
+// conj(psi_r) psi_{r ^ x}.
+//
+// The pair kernel reads the whole state once per group.  Here a work unit
+// (TileChunk) is a set Q of four row bits q0 < q1 < q2 < q3 with up to six
+// groups x = e_{q_i} + e_{q_j} (slot (i, j)): the rows split into 16-row
+// tiles {base + sum_k t_k 2^{q_k}}, and every group of the unit pairs rows
+// inside a tile.  A thread loads a tile's 16 rows of its column once and
+// serves all six groups from registers: 16 loads for 48 row pairs instead
+// of 96, and the row-index arithmetic once per tile.  Row t pairs with
+// t ^ (2^i + 2^j) for t with bit j clear; c = bit i of t.
+//
+// Layout: TC column lanes (one complex element each) x TR = 256 / TC row
+// lanes; grid (units, row splits, column tiles), units fastest, so that
+// concurrent CTAs read the same column tile (sized to stay in L2).
+// float32: tile sums in float32, Kahan-compensated across tiles, float64
+// across threads.  float64: double-float (df64.cuh) on the float32 pipes
+// from the split copy of the state (k_df_split), running df64 sums,
+// float64 across threads; a value outside the df64 range was flagged by
+// the split, and the pair kernel's float64 form recomputes the groups.
+#include "df64.cuh"
+#include "expect_body.cuh"
+
+namespace fpg
+{
+namespace
+{
+
+// slot s <-> the bit positions (i, j), i < j, of its group inside Q
+__constant__ int8_t c_slot_j[kTileSlots] = {1, 2, 2, 3, 3, 3};
+constexpr int kSlotI[kTileSlots] = {0, 0, 1, 0, 1, 2};
+constexpr int kSlotJ[kTileSlots] = {1, 2, 2, 3, 3, 3};
+
+template <typename T> __device__ __forceinline__ void tile_kahan(T &acc, T &cmp, T x)
+{
+    const T y = x - cmp;
+    const T s = acc + y;
+    cmp = (s - acc) - y;
+    acc = s;
+}
+
+// Sums per slot: [slot][c][re, im].  df64 carries (hi, lo) pairs.
+template <bool DF> struct TileAcc;
+
+template <> struct TileAcc<false>
+{
+    float run[kTileSlots][2][2], cmp[kTileSlots][2][2];
+    __device__ void zero()
+    {
+#pragma unroll
+        for (int s = 0; s < kTileSlots; ++s)
+#pragma unroll
+            for (int c = 0; c < 2; ++c)
+                run[s][c][0] = run[s][c][1] = cmp[s][c][0] = cmp[s][c][1] = 0.f;
+    }
+    __device__ double value(int s, int c, int part) const
+    {
+        return (double)run[s][c][part] - (double)cmp[s][c][part];
+    }
+};
+
+template <> struct TileAcc<true>
+{
+    float run[kTileSlots][2][2][2]; // [slot][c][re, im][hi, lo]
+    __device__ void zero()
+    {
+#pragma unroll
+        for (int s = 0; s < kTileSlots; ++s)
+#pragma unroll
+            for (int c = 0; c < 2; ++c)
+                run[s][c][0][0] = run[s][c][0][1] = run[s][c][1][0] = run[s][c][1][1] = 0.f;
+    }
+    __device__ double value(int s, int c, int part) const
+    {
+        return df_to_double(run[s][c][part][0], run[s][c][part][1]);
+    }
+};
+
+// one tile: rows[t] = the tile's row t of this thread's column
+template <int S_>
+__device__ __forceinline__ void tile_slot_f32(const float (&rows)[16][2], float (&ts)[2][2])
+{
+    constexpr int i = kSlotI[S_], j = kSlotJ[S_];
+#pragma unroll
+    for (int t = 0; t < 16; ++t)
+        if (!((t >> j) & 1))
+        {
+            const int u = t ^ ((1 << i) | (1 << j));
+            const int c = (t >> i) & 1;
+            // conj(a) b: re += ar br + ai bi, im += ar bi - ai br
+            ts[c][0] = fmaf(rows[t][0], rows[u][0], fmaf(rows[t][1], rows[u][1], ts[c][0]));
+            ts[c][1] = fmaf(rows[t][0], rows[u][1], fmaf(-rows[t][1], rows[u][0], ts[c][1]));
+        }
+}
+
+template <int S_> __device__ __forceinline__ void tile_slot_df(const float (&rows)[16][4], float (&acc)[2][2][2])
+{
+    constexpr int i = kSlotI[S_], j = kSlotJ[S_];
+#pragma unroll
+    for (int t = 0; t < 16; ++t)
+        if (!((t >> j) & 1))
+        {
+            const int u = t ^ ((1 << i) | (1 << j));
+            const int c = (t >> i) & 1;
+            const float(&a)[4] = rows[t];
+            const float(&b)[4] = rows[u];
+            df_fma(a[0], a[1], b[0], b[1], acc[c][0][0], acc[c][0][1]);
+            df_fma(a[2], a[3], b[2], b[3], acc[c][0][0], acc[c][0][1]);
+            df_fma(a[0], a[1], b[2], b[3], acc[c][1][0], acc[c][1][1]);
+            df_fma(-a[2], -a[3], b[0], b[1], acc[c][1][0], acc[c][1][1]);
+        }
+}
+
+template <int S_> __device__ __forceinline__ void run_slot_f32(const float (&rows)[16][2], TileAcc<false> &A, int act)
+{
+    if (!((act >> S_) & 1))
+        return;
+    float ts[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    tile_slot_f32<S_>(rows, ts);
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+#pragma unroll
+        for (int p = 0; p < 2; ++p)
+            tile_kahan(A.run[S_][c][p], A.cmp[S_][c][p], ts[c][p]);
+}
+
+template <int S_> __device__ __forceinline__ void run_slot_df(const float (&rows)[16][4], TileAcc<true> &A, int act)
+{
+    if (!((act >> S_) & 1))
+        return;
+    tile_slot_df<S_>(rows, A.run[S_]);
+}
+
+// DF: psi = the df64 split copy (float4 per element); else float2 elements
+template <bool DF>
+__global__ void __launch_bounds__(256, DF ? 1 : 2)
+    k_expect_tile(const void *__restrict__ psi, int64_t S, int n, const StringRec *__restrict__ recs,
+                  const int32_t *__restrict__ orig, int64_t P, const TileChunk *__restrict__ units, int TC,
+                  int n_splits, double *__restrict__ out)
+{
+    extern __shared__ double red[]; // 256 * 4 * kTileSlots doubles
+    __shared__ int64_t s_off[16];
+    const TileChunk u = units[blockIdx.x];
+    const int tid = threadIdx.x;
+    const int tc = tid & (TC - 1);
+    const int tr = tid / TC;
+    const int TR = blockDim.x / TC;
+    const int64_t t0 = (int64_t)blockIdx.z * TC + tc;
+    const bool col_ok = t0 < S;
+    const int q0 = u.q[0], q1 = u.q[1], q2 = u.q[2], q3 = u.q[3];
+    if (tid < 16)
+        s_off[tid] = (int64_t)(((uint64_t)(tid & 1) << q0) | ((uint64_t)((tid >> 1) & 1) << q1) |
+                               ((uint64_t)((tid >> 2) & 1) << q2) | ((uint64_t)((tid >> 3) & 1) << q3)) *
+                     S;
+    int act = 0;
+#pragma unroll
+    for (int s = 0; s < kTileSlots; ++s)
+        act |= (u.count[s] > 0) ? (1 << s) : 0;
+    __syncthreads();
+
+    const int64_t nb = (int64_t)1 << (n - 4); // tiles
+    const int64_t per = (nb + n_splits - 1) / n_splits;
+    const int64_t b0 = (int64_t)blockIdx.y * per;
+    const int64_t b1 = min(nb, b0 + per);
+
+    TileAcc<DF> A;
+    A.zero();
+    if (col_ok)
+    {
+        [[maybe_unused]] int since_norm = 0;
+        for (int64_t m = b0 + tr; m < b1; m += TR)
+        {
+            // base: m with zero bits inserted at q0 < q1 < q2 < q3
+            uint64_t base = (uint64_t)m;
+            base = ((base >> q0) << (q0 + 1)) | (base & ((1ull << q0) - 1ull));
+            base = ((base >> q1) << (q1 + 1)) | (base & ((1ull << q1) - 1ull));
+            base = ((base >> q2) << (q2 + 1)) | (base & ((1ull << q2) - 1ull));
+            base = ((base >> q3) << (q3 + 1)) | (base & ((1ull << q3) - 1ull));
+            const int64_t e0 = (int64_t)base * S + t0;
+            if constexpr (DF)
+            {
+                float rows[16][4];
+#pragma unroll
+                for (int t = 0; t < 16; ++t)
+                {
+                    const float4 v = __ldg(reinterpret_cast<const float4 *>(psi) + e0 + s_off[t]);
+                    rows[t][0] = v.x;
+                    rows[t][1] = v.y;
+                    rows[t][2] = v.z;
+                    rows[t][3] = v.w;
+                }
+                run_slot_df<0>(rows, A, act);
+                run_slot_df<1>(rows, A, act);
+                run_slot_df<2>(rows, A, act);
+                run_slot_df<3>(rows, A, act);
+                run_slot_df<4>(rows, A, act);
+                run_slot_df<5>(rows, A, act);
+                // each sum took 8 df64 terms: renormalise every 4 tiles
+                if (++since_norm == 4)
+                {
+                    since_norm = 0;
+#pragma unroll
+                    for (int s = 0; s < kTileSlots; ++s)
+#pragma unroll
+                        for (int c = 0; c < 2; ++c)
+#pragma unroll
+                            for (int p = 0; p < 2; ++p)
+                                df_norm(A.run[s][c][p][0], A.run[s][c][p][1]);
+                }
+            }
+            else
+            {
+                float rows[16][2];
+#pragma unroll
+                for (int t = 0; t < 16; ++t)
+                {
+                    const float2 v = __ldg(reinterpret_cast<const float2 *>(psi) + e0 + s_off[t]);
+                    rows[t][0] = v.x;
+                    rows[t][1] = v.y;
+                }
+                run_slot_f32<0>(rows, A, act);
+                run_slot_f32<1>(rows, A, act);
+                run_slot_f32<2>(rows, A, act);
+                run_slot_f32<3>(rows, A, act);
+                run_slot_f32<4>(rows, A, act);
+                run_slot_f32<5>(rows, A, act);
+            }
+        }
+    }
+
+    // the 4 x 6 sums of every thread into shared memory, summed over the row
+    // lanes in a fixed order (deterministic), then one thread per (column,
+    // slot) writes the slot's strings
+    constexpr int NQ = 4 * kTileSlots;
+#pragma unroll
+    for (int s = 0; s < kTileSlots; ++s)
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+#pragma unroll
+            for (int p = 0; p < 2; ++p)
+                red[(size_t)tid * NQ + s * 4 + p * 2 + c] = A.value(s, c, p);
+    __syncthreads();
+    // tot[tc][q] into the slots of row lane 0
+    for (int k = tid; k < TC * NQ; k += blockDim.x)
+    {
+        const int c = k / NQ, q = k - c * NQ;
+        double v = 0.0;
+        for (int r = 0; r < TR; ++r)
+            v += red[(size_t)(r * TC + c) * NQ + q];
+        red[(size_t)(TR * TC) * NQ + k] = v;
+    }
+    __syncthreads();
+    if (tid >= TC * kTileSlots)
+        return;
+    const int c = tid % TC, s = tid / TC;
+    const int64_t col = (int64_t)blockIdx.z * TC + c;
+    if (col >= S || u.count[s] == 0)
+        return;
+    const double *tot = red + (size_t)(TR * TC) * NQ + (size_t)c * NQ + s * 4; // re c0, re c1, im c0, im c1
+    const uint64_t pbit = 1ull << u.q[c_slot_j[s]];
+    for (int k = 0; k < u.count[s]; ++k)
+    {
+        const int sidx = u.begin[s] + k;
+        const StringRec rec = recs[sidx];
+        const bool odd = (rec.meta & 1u) != 0;
+        const bool flip = (rec.z & ~pbit) != 0; // z' = e_a
+        const double f = ((rec.meta & 2u) ? -2.0 : 2.0);
+        const double u0 = odd ? tot[2] : tot[0];
+        const double u1 = odd ? tot[3] : tot[1];
+        out[((int64_t)blockIdx.y * P + orig[sidx]) * S + col] = f * (flip ? u0 - u1 : u0 + u1);
+    }
+}
+
+} // namespace
+
+size_t tile_smem_bytes(int TC)
+{
+    // every thread's sums, then the column totals
+    return (size_t)(256 + TC) * 4 * kTileSlots * sizeof(double);
+}
+
+cudaError_t launch_expect_tile(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const TileChunk *d_units,
+                               int n_units, int TC, int n_ctiles, int n_splits, double *out, cudaStream_t st)
+{
+    if (n_units <= 0)
+        return cudaSuccess;
+    dim3 grid((unsigned)n_units, (unsigned)n_splits, (unsigned)n_ctiles);
+    const size_t smem = tile_smem_bytes(TC);
+    if (fp32)
+    {
+        if (cudaError_t e = cudaFuncSetAttribute(k_expect_tile<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem))
+            return e;
+        k_expect_tile<false><<<grid, 256, smem, st>>>(psi, S, n, op.recs, op.orig, op.P, d_units, TC, n_splits, out);
+    }
+    else
+    {
+        if (cudaError_t e = cudaFuncSetAttribute(k_expect_tile<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem))
+            return e;
+        k_expect_tile<true><<<grid, 256, smem, st>>>(psi, S, n, op.recs, op.orig, op.P, d_units, TC, n_splits, out);
+    }
+    return launched();
+}
+
+} // namespace fpg
