@@ -83,21 +83,32 @@ template <> struct TileAcc<true>
     }
 };
 
-// one tile: rows[t] = the tile's row t of this thread's column
+// one tile: rows[t] = the tile's row t of this thread's column.  float32:
+// the four products of conj(a) b in separate sums per c (eight independent
+// FMA chains per slot), combined once per tile
 template <int S_>
 __device__ __forceinline__ void tile_slot_f32(const float (&rows)[16][2], float (&ts)[2][2])
 {
     constexpr int i = kSlotI[S_], j = kSlotJ[S_];
+    float rr[2] = {0.f, 0.f}, ii[2] = {0.f, 0.f}, ri[2] = {0.f, 0.f}, ir[2] = {0.f, 0.f};
 #pragma unroll
     for (int t = 0; t < 16; ++t)
         if (!((t >> j) & 1))
         {
             const int u = t ^ ((1 << i) | (1 << j));
             const int c = (t >> i) & 1;
-            // conj(a) b: re += ar br + ai bi, im += ar bi - ai br
-            ts[c][0] = fmaf(rows[t][0], rows[u][0], fmaf(rows[t][1], rows[u][1], ts[c][0]));
-            ts[c][1] = fmaf(rows[t][0], rows[u][1], fmaf(-rows[t][1], rows[u][0], ts[c][1]));
+            // conj(a) b: re = ar br + ai bi, im = ar bi - ai br
+            rr[c] = fmaf(rows[t][0], rows[u][0], rr[c]);
+            ii[c] = fmaf(rows[t][1], rows[u][1], ii[c]);
+            ri[c] = fmaf(rows[t][0], rows[u][1], ri[c]);
+            ir[c] = fmaf(-rows[t][1], rows[u][0], ir[c]);
         }
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+    {
+        ts[c][0] = rr[c] + ii[c];
+        ts[c][1] = ri[c] + ir[c];
+    }
 }
 
 template <int S_> __device__ __forceinline__ void tile_slot_df(const float (&rows)[16][4], float (&acc)[2][2][2])
@@ -122,7 +133,7 @@ template <int S_> __device__ __forceinline__ void run_slot_f32(const float (&row
 {
     if (!((act >> S_) & 1))
         return;
-    float ts[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    float ts[2][2];
     tile_slot_f32<S_>(rows, ts);
 #pragma unroll
     for (int c = 0; c < 2; ++c)
@@ -145,7 +156,7 @@ __global__ void __launch_bounds__(256, DF ? 1 : 2)
                   const int32_t *__restrict__ orig, int64_t P, const TileChunk *__restrict__ units, int TC,
                   int n_splits, double *__restrict__ out)
 {
-    extern __shared__ double red[]; // 256 * 4 * kTileSlots doubles
+    extern __shared__ double red[]; // (256 + TC) * 4 * kTileSlots doubles
     __shared__ int64_t s_off[16];
     const TileChunk u = units[blockIdx.x];
     const int tid = threadIdx.x;
