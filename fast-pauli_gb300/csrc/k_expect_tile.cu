@@ -46,16 +46,16 @@ template <typename T> __device__ __forceinline__ void tile_kahan(T &acc, T &cmp,
     acc = s;
 }
 
-// Sums per slot: [slot][c][re, im].  df64 carries (hi, lo) pairs.
-template <bool DF> struct TileAcc;
+// Sums of NS slots: [slot][c][re, im].  df64 carries (hi, lo) pairs.
+template <bool DF, int NS> struct TileAcc;
 
-template <> struct TileAcc<false>
+template <int NS> struct TileAcc<false, NS>
 {
-    float run[kTileSlots][2][2], cmp[kTileSlots][2][2];
+    float run[NS][2][2], cmp[NS][2][2];
     __device__ void zero()
     {
 #pragma unroll
-        for (int s = 0; s < kTileSlots; ++s)
+        for (int s = 0; s < NS; ++s)
 #pragma unroll
             for (int c = 0; c < 2; ++c)
                 run[s][c][0] = run[s][c][1] = cmp[s][c][0] = cmp[s][c][1] = 0.f;
@@ -66,13 +66,13 @@ template <> struct TileAcc<false>
     }
 };
 
-template <> struct TileAcc<true>
+template <int NS> struct TileAcc<true, NS>
 {
-    float run[kTileSlots][2][2][2]; // [slot][c][re, im][hi, lo]
+    float run[NS][2][2][2]; // [slot][c][re, im][hi, lo]
     __device__ void zero()
     {
 #pragma unroll
-        for (int s = 0; s < kTileSlots; ++s)
+        for (int s = 0; s < NS; ++s)
 #pragma unroll
             for (int c = 0; c < 2; ++c)
                 run[s][c][0][0] = run[s][c][0][1] = run[s][c][1][0] = run[s][c][1][1] = 0.f;
@@ -80,6 +80,16 @@ template <> struct TileAcc<true>
     __device__ double value(int s, int c, int part) const
     {
         return df_to_double(run[s][c][part][0], run[s][c][part][1]);
+    }
+    __device__ void norm()
+    {
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+#pragma unroll
+            for (int c = 0; c < 2; ++c)
+#pragma unroll
+                for (int p = 0; p < 2; ++p)
+                    df_norm(run[s][c][p][0], run[s][c][p][1]);
     }
 };
 
@@ -129,9 +139,11 @@ template <int S_> __device__ __forceinline__ void tile_slot_df(const float (&row
         }
 }
 
-template <int S_> __device__ __forceinline__ void run_slot_f32(const float (&rows)[16][2], TileAcc<false> &A, int act)
+// slot S_ of the unit into local accumulator L_, if active
+template <int S_, int L_, int NS>
+__device__ __forceinline__ void run_slot(const float (&rows)[16][2], TileAcc<false, NS> &A, int act)
 {
-    if (!((act >> S_) & 1))
+    if (!((act >> L_) & 1))
         return;
     float ts[2][2];
     tile_slot_f32<S_>(rows, ts);
@@ -139,26 +151,65 @@ template <int S_> __device__ __forceinline__ void run_slot_f32(const float (&row
     for (int c = 0; c < 2; ++c)
 #pragma unroll
         for (int p = 0; p < 2; ++p)
-            tile_kahan(A.run[S_][c][p], A.cmp[S_][c][p], ts[c][p]);
+            tile_kahan(A.run[L_][c][p], A.cmp[L_][c][p], ts[c][p]);
 }
 
-template <int S_> __device__ __forceinline__ void run_slot_df(const float (&rows)[16][4], TileAcc<true> &A, int act)
+template <int S_, int L_, int NS>
+__device__ __forceinline__ void run_slot(const float (&rows)[16][4], TileAcc<true, NS> &A, int act)
 {
-    if (!((act >> S_) & 1))
+    if (!((act >> L_) & 1))
         return;
-    tile_slot_df<S_>(rows, A.run[S_]);
+    tile_slot_df<S_>(rows, A.run[L_]);
 }
 
-// DF: psi = the df64 split copy (float4 per element); else float2 elements
-template <bool DF>
-__global__ void __launch_bounds__(256, DF ? 1 : 2)
+// the NS slots of this CTA: all six, or the half sb / 3
+template <int NS, typename Rows, typename Acc>
+__device__ __forceinline__ void run_slots(const Rows &rows, Acc &A, int act, int sb)
+{
+    if constexpr (NS == kTileSlots)
+    {
+        run_slot<0, 0>(rows, A, act);
+        run_slot<1, 1>(rows, A, act);
+        run_slot<2, 2>(rows, A, act);
+        run_slot<3, 3>(rows, A, act);
+        run_slot<4, 4>(rows, A, act);
+        run_slot<5, 5>(rows, A, act);
+    }
+    else if (sb == 0)
+    {
+        run_slot<0, 0>(rows, A, act);
+        run_slot<1, 1>(rows, A, act);
+        run_slot<2, 2>(rows, A, act);
+    }
+    else
+    {
+        run_slot<3, 0>(rows, A, act);
+        run_slot<4, 1>(rows, A, act);
+        run_slot<5, 2>(rows, A, act);
+    }
+}
+
+template <bool DF, int NS> constexpr int kTileMinBlocks = DF ? (NS == kTileSlots ? 1 : 2) : (NS == kTileSlots ? 2 : 3);
+
+// DF: psi = the df64 split copy (float4 per element); else float2 elements.
+// NS = 6: one CTA per unit; NS = 3: two CTAs per unit (blockIdx.x = 2 unit +
+// half), each with half the slots and half the accumulator registers.
+template <bool DF, int NS>
+__global__ void __launch_bounds__(256, kTileMinBlocks<DF, NS>)
     k_expect_tile(const void *__restrict__ psi, int64_t S, int n, const StringRec *__restrict__ recs,
                   const int32_t *__restrict__ orig, int64_t P, const TileChunk *__restrict__ units, int TC,
                   int n_splits, double *__restrict__ out)
 {
-    extern __shared__ double red[]; // (256 + TC) * 4 * kTileSlots doubles
+    extern __shared__ double red[]; // (256 + TC) * 4 * NS doubles
     __shared__ int64_t s_off[16];
-    const TileChunk u = units[blockIdx.x];
+    const TileChunk u = units[NS == kTileSlots ? blockIdx.x : blockIdx.x >> 1];
+    const int sb = NS == kTileSlots ? 0 : (int)(blockIdx.x & 1) * NS; // first slot of this CTA
+    int act = 0;
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+        act |= (u.count[sb + s] > 0) ? (1 << s) : 0;
+    if (act == 0)
+        return; // a half without groups (uniform over the CTA)
     const int tid = threadIdx.x;
     const int tc = tid & (TC - 1);
     const int tr = tid / TC;
@@ -170,10 +221,6 @@ __global__ void __launch_bounds__(256, DF ? 1 : 2)
         s_off[tid] = (int64_t)(((uint64_t)(tid & 1) << q0) | ((uint64_t)((tid >> 1) & 1) << q1) |
                                ((uint64_t)((tid >> 2) & 1) << q2) | ((uint64_t)((tid >> 3) & 1) << q3)) *
                      S;
-    int act = 0;
-#pragma unroll
-    for (int s = 0; s < kTileSlots; ++s)
-        act |= (u.count[s] > 0) ? (1 << s) : 0;
     __syncthreads();
 
     const int64_t nb = (int64_t)1 << (n - 4); // tiles
@@ -181,7 +228,7 @@ __global__ void __launch_bounds__(256, DF ? 1 : 2)
     const int64_t b0 = (int64_t)blockIdx.y * per;
     const int64_t b1 = min(nb, b0 + per);
 
-    TileAcc<DF> A;
+    TileAcc<DF, NS> A;
     A.zero();
     if (col_ok)
     {
@@ -207,23 +254,12 @@ __global__ void __launch_bounds__(256, DF ? 1 : 2)
                     rows[t][2] = v.z;
                     rows[t][3] = v.w;
                 }
-                run_slot_df<0>(rows, A, act);
-                run_slot_df<1>(rows, A, act);
-                run_slot_df<2>(rows, A, act);
-                run_slot_df<3>(rows, A, act);
-                run_slot_df<4>(rows, A, act);
-                run_slot_df<5>(rows, A, act);
+                run_slots<NS>(rows, A, act, sb);
                 // each sum took 8 df64 terms: renormalise every 4 tiles
                 if (++since_norm == 4)
                 {
                     since_norm = 0;
-#pragma unroll
-                    for (int s = 0; s < kTileSlots; ++s)
-#pragma unroll
-                        for (int c = 0; c < 2; ++c)
-#pragma unroll
-                            for (int p = 0; p < 2; ++p)
-                                df_norm(A.run[s][c][p][0], A.run[s][c][p][1]);
+                    A.norm();
                 }
             }
             else
@@ -236,29 +272,24 @@ __global__ void __launch_bounds__(256, DF ? 1 : 2)
                     rows[t][0] = v.x;
                     rows[t][1] = v.y;
                 }
-                run_slot_f32<0>(rows, A, act);
-                run_slot_f32<1>(rows, A, act);
-                run_slot_f32<2>(rows, A, act);
-                run_slot_f32<3>(rows, A, act);
-                run_slot_f32<4>(rows, A, act);
-                run_slot_f32<5>(rows, A, act);
+                run_slots<NS>(rows, A, act, sb);
             }
         }
     }
 
-    // the 4 x 6 sums of every thread into shared memory, summed over the row
+    // the 4 x NS sums of every thread into shared memory, summed over the row
     // lanes in a fixed order (deterministic), then one thread per (column,
     // slot) writes the slot's strings
-    constexpr int NQ = 4 * kTileSlots;
+    constexpr int NQ = 4 * NS;
 #pragma unroll
-    for (int s = 0; s < kTileSlots; ++s)
+    for (int s = 0; s < NS; ++s)
 #pragma unroll
         for (int c = 0; c < 2; ++c)
 #pragma unroll
             for (int p = 0; p < 2; ++p)
                 red[(size_t)tid * NQ + s * 4 + p * 2 + c] = A.value(s, c, p);
     __syncthreads();
-    // tot[tc][q] into the slots of row lane 0
+    // tot[tc][q] after every thread's sums
     for (int k = tid; k < TC * NQ; k += blockDim.x)
     {
         const int c = k / NQ, q = k - c * NQ;
@@ -268,13 +299,13 @@ __global__ void __launch_bounds__(256, DF ? 1 : 2)
         red[(size_t)(TR * TC) * NQ + k] = v;
     }
     __syncthreads();
-    if (tid >= TC * kTileSlots)
+    if (tid >= TC * NS)
         return;
-    const int c = tid % TC, s = tid / TC;
+    const int c = tid % TC, ls = tid / TC, s = sb + ls;
     const int64_t col = (int64_t)blockIdx.z * TC + c;
     if (col >= S || u.count[s] == 0)
         return;
-    const double *tot = red + (size_t)(TR * TC) * NQ + (size_t)c * NQ + s * 4; // re c0, re c1, im c0, im c1
+    const double *tot = red + (size_t)(TR * TC) * NQ + (size_t)c * NQ + ls * 4; // re c0, re c1, im c0, im c1
     const uint64_t pbit = 1ull << u.q[c_slot_j[s]];
     for (int k = 0; k < u.count[s]; ++k)
     {
@@ -289,36 +320,33 @@ __global__ void __launch_bounds__(256, DF ? 1 : 2)
     }
 }
 
-} // namespace
-
-size_t tile_smem_bytes(int TC)
+template <bool DF, int NS>
+cudaError_t launch_tile(const void *psi, int64_t S, int n, const DevOp &op, const TileChunk *d_units, int n_units,
+                        int TC, int n_ctiles, int n_splits, double *out, cudaStream_t st)
 {
-    // every thread's sums, then the column totals
-    return (size_t)(256 + TC) * 4 * kTileSlots * sizeof(double);
+    dim3 grid((unsigned)(n_units * (kTileSlots / NS)), (unsigned)n_splits, (unsigned)n_ctiles);
+    const size_t smem = (size_t)(256 + TC) * 4 * NS * sizeof(double);
+    if (cudaError_t e = cudaFuncSetAttribute(k_expect_tile<DF, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem))
+        return e;
+    k_expect_tile<DF, NS><<<grid, 256, smem, st>>>(psi, S, n, op.recs, op.orig, op.P, d_units, TC, n_splits, out);
+    return launched();
 }
+
+} // namespace
 
 cudaError_t launch_expect_tile(bool fp32, const void *psi, int64_t S, int n, const DevOp &op, const TileChunk *d_units,
                                int n_units, int TC, int n_ctiles, int n_splits, double *out, cudaStream_t st)
 {
     if (n_units <= 0)
         return cudaSuccess;
-    dim3 grid((unsigned)n_units, (unsigned)n_splits, (unsigned)n_ctiles);
-    const size_t smem = tile_smem_bytes(TC);
+    // float32: one CTA per unit (128 registers, two CTAs per SM; halves, at
+    // three CTAs per SM, ran 1.22x slower); float64: two CTAs per unit, so
+    // that the accumulators of three slots fit two CTAs per SM (six slots
+    // take 238 registers: one CTA per SM, 1.01x slower per step)
     if (fp32)
-    {
-        if (cudaError_t e = cudaFuncSetAttribute(k_expect_tile<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem))
-            return e;
-        k_expect_tile<false><<<grid, 256, smem, st>>>(psi, S, n, op.recs, op.orig, op.P, d_units, TC, n_splits, out);
-    }
-    else
-    {
-        if (cudaError_t e = cudaFuncSetAttribute(k_expect_tile<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem))
-            return e;
-        k_expect_tile<true><<<grid, 256, smem, st>>>(psi, S, n, op.recs, op.orig, op.P, d_units, TC, n_splits, out);
-    }
-    return launched();
+        return launch_tile<false, 6>(psi, S, n, op, d_units, n_units, TC, n_ctiles, n_splits, out, st);
+    return launch_tile<true, 3>(psi, S, n, op, d_units, n_units, TC, n_ctiles, n_splits, out, st);
 }
 
 } // namespace fpg
