@@ -126,6 +126,55 @@ def test_large_n_weight2_subset(n, S):
     assert normwise(sop.apply_weighted(psi, data), oracle.summed_apply_weighted(strings, h, psi, data)) < TOL_C128
 
 
+def _two_position_strings(n, pairs, kinds=("XX", "XY", "YX", "YY")):
+    out = []
+    for a, b in pairs:  # qubit positions (string index), a < b
+        for k in kinds:
+            s = ["I"] * n
+            s[a], s[b] = k[0], k[1]
+            out.append("".join(s))
+    return out
+
+
+@pytest.mark.parametrize(
+    "case,n,S",
+    [("tiles_and_pairs", 10, 9), ("few_groups", 10, 6), ("below_min_qubits", 7, 5), ("pairs_past_l2", 20, 4)],
+)
+@pytest.mark.parametrize("c64", [False, True])
+def test_two_position_groups_tile_and_pair_kernels(case, n, S, c64):
+    """The two-position x-groups (XX, XY, YX, YY on two qubits) go to the tile
+    kernel, several per pass, when at least six of them have signs only on
+    their lower qubit; the rest, and every such group of an operator on
+    fewer than eight qubits, stay with the pair kernel; a state whose column
+    tile does not fit in L2 runs the tile groups through the pair kernel."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(hash(case) % 1000 + n)
+    every_pair = [(a, b) for a in range(n) for b in range(a + 1, n)]
+    if case == "tiles_and_pairs":
+        strings = _two_position_strings(n, every_pair[:20])
+        # X X Z on three qubits with X X: signs on a third qubit (pair kernel)
+        for a, b, c in [(0, 5, 8), (2, 3, 9), (4, 7, 1)]:
+            s = ["I"] * n
+            s[a], s[b] = "X", "X"
+            strings.append("".join(s))
+            s[c] = "Z"
+            strings.append("".join(s))
+        strings += ["Z" + "I" * (n - 1), "X" + "I" * (n - 1)]
+    elif case == "few_groups":
+        strings = _two_position_strings(n, every_pair[:5])
+    elif case == "below_min_qubits":
+        strings = _two_position_strings(n, every_pair)
+    else:
+        strings = _two_position_strings(n, every_pair[::17][:10])
+    P, K = len(strings), 3
+    h = (rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))) / np.sqrt(2 * P)
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    want = oracle.summed_expectation(strings, h, psi)
+    states = torch.from_numpy(psi).to(torch.complex64 if c64 else torch.complex128).cuda()
+    got = fp.SummedPauliOp(strings, h).expectation_value(states).cpu().numpy()
+    assert normwise(got, want) < (TOL_MIXED if c64 else TOL_C128)
+
+
 @pytest.mark.parametrize("kind", ["weight2", "uniform", "weight2_c64", "weight2_tiny"])
 def test_pinned_host_states(kind):
     """Pinned host states (as torch's pinned tensors give them): float64 and
