@@ -60,9 +60,10 @@ template <int NS> struct TileAcc<false, NS>
             for (int c = 0; c < 2; ++c)
                 run[s][c][0] = run[s][c][1] = cmp[s][c][0] = cmp[s][c][1] = 0.f;
     }
-    __device__ double value(int s, int c, int part) const
+    // the compensated sum as an unevaluated pair hi + lo
+    __device__ float2 pair(int s, int c, int part) const
     {
-        return (double)run[s][c][part] - (double)cmp[s][c][part];
+        return make_float2(run[s][c][part], -cmp[s][c][part]);
     }
 };
 
@@ -77,9 +78,9 @@ template <int NS> struct TileAcc<true, NS>
             for (int c = 0; c < 2; ++c)
                 run[s][c][0][0] = run[s][c][0][1] = run[s][c][1][0] = run[s][c][1][1] = 0.f;
     }
-    __device__ double value(int s, int c, int part) const
+    __device__ float2 pair(int s, int c, int part) const
     {
-        return df_to_double(run[s][c][part][0], run[s][c][part][1]);
+        return make_float2(run[s][c][part][0], run[s][c][part][1]);
     }
     __device__ void norm()
     {
@@ -200,7 +201,7 @@ __global__ void __launch_bounds__(256, kTileMinBlocks<DF, NS>)
                   const int32_t *__restrict__ orig, int64_t P, const TileChunk *__restrict__ units, int TC,
                   int n_splits, double *__restrict__ out)
 {
-    extern __shared__ double red[]; // (256 + TC) * 4 * NS doubles
+    extern __shared__ double red[]; // 256 * 4 * NS float pairs, then TC * 4 * NS doubles
     __shared__ int64_t s_off[16];
     const TileChunk u = units[NS == kTileSlots ? blockIdx.x : blockIdx.x >> 1];
     const int sb = NS == kTileSlots ? 0 : (int)(blockIdx.x & 1) * NS; // first slot of this CTA
@@ -277,26 +278,31 @@ __global__ void __launch_bounds__(256, kTileMinBlocks<DF, NS>)
         }
     }
 
-    // the 4 x NS sums of every thread into shared memory, summed over the row
-    // lanes in a fixed order (deterministic), then one thread per (column,
-    // slot) writes the slot's strings
+    // the 4 x NS sums of every thread into shared memory as (hi, lo) float
+    // pairs, summed over the row lanes in a fixed order (deterministic) in
+    // double-float on the float32 pipes; only the column totals become
+    // float64.  Then one thread per (column, slot) writes the slot's strings.
     constexpr int NQ = 4 * NS;
+    float2 *pr = reinterpret_cast<float2 *>(red);
 #pragma unroll
     for (int s = 0; s < NS; ++s)
 #pragma unroll
         for (int c = 0; c < 2; ++c)
 #pragma unroll
             for (int p = 0; p < 2; ++p)
-                red[(size_t)tid * NQ + s * 4 + p * 2 + c] = A.value(s, c, p);
+                pr[(size_t)tid * NQ + s * 4 + p * 2 + c] = A.pair(s, c, p);
     __syncthreads();
-    // tot[tc][q] after every thread's sums
+    double *tots = red + (size_t)(TR * TC) * NQ / 2; // after the pairs
     for (int k = tid; k < TC * NQ; k += blockDim.x)
     {
         const int c = k / NQ, q = k - c * NQ;
-        double v = 0.0;
+        float h = 0.f, l = 0.f;
         for (int r = 0; r < TR; ++r)
-            v += red[(size_t)(r * TC + c) * NQ + q];
-        red[(size_t)(TR * TC) * NQ + k] = v;
+        {
+            const float2 v = pr[(size_t)(r * TC + c) * NQ + q];
+            df_add(h, l, v.x, v.y);
+        }
+        tots[k] = df_to_double(h, l);
     }
     __syncthreads();
     if (tid >= TC * NS)
@@ -305,7 +311,7 @@ __global__ void __launch_bounds__(256, kTileMinBlocks<DF, NS>)
     const int64_t col = (int64_t)blockIdx.z * TC + c;
     if (col >= S || u.count[s] == 0)
         return;
-    const double *tot = red + (size_t)(TR * TC) * NQ + (size_t)c * NQ + ls * 4; // re c0, re c1, im c0, im c1
+    const double *tot = tots + (size_t)c * NQ + ls * 4; // re c0, re c1, im c0, im c1
     const uint64_t pbit = 1ull << u.q[c_slot_j[s]];
     for (int k = 0; k < u.count[s]; ++k)
     {
@@ -325,7 +331,8 @@ cudaError_t launch_tile(const void *psi, int64_t S, int n, const DevOp &op, cons
                         int TC, int n_ctiles, int n_splits, double *out, cudaStream_t st)
 {
     dim3 grid((unsigned)(n_units * (kTileSlots / NS)), (unsigned)n_splits, (unsigned)n_ctiles);
-    const size_t smem = (size_t)(256 + TC) * 4 * NS * sizeof(double);
+    // every thread's (hi, lo) pairs, then the column totals
+    const size_t smem = (size_t)256 * 4 * NS * sizeof(float2) + (size_t)TC * 4 * NS * sizeof(double);
     if (cudaError_t e = cudaFuncSetAttribute(k_expect_tile<DF, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem))
         return e;
