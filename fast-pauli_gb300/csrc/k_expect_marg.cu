@@ -76,6 +76,12 @@ struct ArF32
     {
         return (double)a.v - (double)a.c;
     }
+    // the row-lane reduction in double-float pairs (hi, lo) on the float32 pipes
+    static constexpr bool kPairReduce = true;
+    static __device__ __forceinline__ float2 to_pair(const acc &a)
+    {
+        return make_float2(a.v, -a.c);
+    }
     // a += b (both compensated: b's sum is b.v - b.c)
     static __device__ __forceinline__ void acc_merge(acc &a, const acc &b)
     {
@@ -164,6 +170,11 @@ struct ArF64
     {
         return a;
     }
+    static constexpr bool kPairReduce = false;
+    static __device__ __forceinline__ float2 to_pair(const acc &)
+    {
+        return make_float2(0.f, 0.f);
+    }
     static __device__ __forceinline__ acc from2(float2 f)
     {
         return (double)__hiloint2double(__float_as_int(f.y), __float_as_int(f.x));
@@ -225,6 +236,11 @@ struct ArDF
     static __device__ __forceinline__ double to_double(const acc &a)
     {
         return df_to_double(a.h, a.l);
+    }
+    static constexpr bool kPairReduce = true;
+    static __device__ __forceinline__ float2 to_pair(const acc &a)
+    {
+        return make_float2(a.h, a.l);
     }
     static __device__ __forceinline__ acc from2(float2 f)
     {
@@ -516,7 +532,49 @@ __global__ void __launch_bounds__(256, 2)
 
     if (A::kRaises && bad)
         atomicOr(range_flag, 1);
-    // deterministic float64 reduction over the row lanes, NVB values a pass
+    // deterministic reduction over the row lanes, NVB values a pass: in
+    // double-float pairs on the float32 pipes (float64 only for the column
+    // totals), or in float64 for the float64 accumulators
+    if constexpr (A::kPairReduce)
+    {
+        float2 *rp = reinterpret_cast<float2 *>(red);
+#pragma unroll
+        for (int v0 = 0; v0 < NV; v0 += NVB)
+        {
+#pragma unroll
+            for (int w = 0; w < NVB; ++w)
+            {
+                const int v = v0 + w;
+                if (v < NV)
+                {
+                    const int p = v / (NV / 2), i = v % (NV / 2);
+                    rp[w * 256 + tid] = A::to_pair(
+                        i == 0 ? tot[p] : (i < 6 ? ml[p][i - 1] : A::from2(smh[(p * NH + i - 6) * 256 + tid])));
+                }
+            }
+            __syncthreads();
+            for (int s = TR >> 1; s > 0; s >>= 1)
+            {
+                if (tr < s)
+#pragma unroll
+                    for (int w = 0; w < NVB; ++w)
+                    {
+                        float2 x = rp[w * 256 + tid];
+                        const float2 y = rp[w * 256 + tid + s * TC];
+                        df_add(x.x, x.y, y.x, y.y);
+                        rp[w * 256 + tid] = x;
+                    }
+                __syncthreads();
+            }
+            if (tr == 0)
+#pragma unroll
+                for (int w = 0; w < NVB; ++w)
+                    if (v0 + w < NV)
+                        res[(v0 + w) * TC + tc] = df_to_double(rp[w * 256 + tc].x, rp[w * 256 + tc].y);
+            __syncthreads();
+        }
+    }
+    else
 #pragma unroll
     for (int v0 = 0; v0 < NV; v0 += NVB)
     {
