@@ -84,6 +84,30 @@ __device__ __forceinline__ void df_fma(float xh, float xl, float yh, float yl, f
     sl = __fadd_rn(sl, __fadd_rn(err, e));
 }
 
+// (sh, sl) = (xh + xl) * (yh + yl), to ~2^-47 relative of the product: the
+// first term of a sum, with no addition
+__device__ __forceinline__ void df_mul(float xh, float xl, float yh, float yl, float &sh, float &sl)
+{
+    const float p = __fmul_rn(xh, yh);
+    float e = __fmaf_rn(xh, yh, -p);
+    e = __fmaf_rn(xh, yl, e);
+    e = __fmaf_rn(xl, yh, e);
+    sh = p;
+    sl = e;
+}
+
+// (ah, al) += (bh, bl) without renormalising: TwoSum of the high parts, the
+// low part absorbing its error and bl.  Like df_fma the low part grows with
+// each term: callers renormalise (df_norm) every few terms.
+__device__ __forceinline__ void df_add_lazy(float &ah, float &al, float bh, float bl)
+{
+    const float s = __fadd_rn(ah, bh);
+    const float bb = __fsub_rn(s, ah);
+    const float err = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, bb)), __fsub_rn(bh, bb));
+    ah = s;
+    al = __fadd_rn(al, __fadd_rn(err, bl));
+}
+
 // Renormalise (h, l) so that |l| <= ulp(h) / 2 (FastTwoSum).  df_fma lets the
 // low part grow with the number of terms it has absorbed, which costs its
 // rounding ~2^-24 |l| per step: callers renormalise every few dozen terms.

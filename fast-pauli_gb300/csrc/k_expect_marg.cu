@@ -57,6 +57,9 @@ struct ArF32
     {
         a += b;
     }
+    static __device__ __forceinline__ void fix(val &)
+    {
+    }
     static __device__ __forceinline__ val sum(val a, val b)
     {
         return a + b;
@@ -150,6 +153,9 @@ struct ArF64
     {
         a += b;
     }
+    static __device__ __forceinline__ void fix(val &)
+    {
+    }
     static __device__ __forceinline__ val sum(val a, val b)
     {
         return a + b;
@@ -212,14 +218,19 @@ struct ArDF
     {
         return DF{0.f, 0.f};
     }
+    // inside a block: sums without renormalising, fixed at each 16-row half
     static __device__ __forceinline__ void add(val &a, val b)
     {
-        df_add(a.h, a.l, b.h, b.l);
+        df_add_lazy(a.h, a.l, b.h, b.l);
     }
     static __device__ __forceinline__ val sum(val a, val b)
     {
-        df_add(a.h, a.l, b.h, b.l);
+        df_add_lazy(a.h, a.l, b.h, b.l);
         return a;
+    }
+    static __device__ __forceinline__ void fix(val &a)
+    {
+        df_norm(a.h, a.l);
     }
     static __device__ __forceinline__ acc acc_zero()
     {
@@ -262,14 +273,12 @@ struct ArDF
     {
         if (re)
         {
-            vr = DF{0.f, 0.f};
-            df_fma(a.x, a.y, b.x, b.y, vr.h, vr.l);
+            df_mul(a.x, a.y, b.x, b.y, vr.h, vr.l);
             df_fma(a.z, a.w, b.z, b.w, vr.h, vr.l);
         }
         if (im)
         {
-            vi = DF{0.f, 0.f};
-            df_fma(a.x, a.y, b.z, b.w, vi.h, vi.l);
+            df_mul(a.x, a.y, b.z, b.w, vi.h, vi.l);
             df_fma(-a.z, -a.w, b.x, b.y, vi.h, vi.l);
         }
     }
@@ -382,6 +391,10 @@ __device__ __forceinline__ void block_marginals(const typename A::in_t *__restri
             A::add(bt[p], hs[p]);
             if (h)
                 A::add(bl[p][4], hs[p]);
+            A::fix(bt[p]);
+#pragma unroll
+            for (int j = 0; j < 5; ++j)
+                A::fix(bl[p][j]);
         }
     }
 }

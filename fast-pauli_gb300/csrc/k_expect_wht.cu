@@ -170,27 +170,28 @@ struct WDF
     {
         if (re)
         {
-            vr = DFv{0.f, 0.f};
-            df_fma(a.x, a.y, b.x, b.y, vr.h, vr.l);
+            df_mul(a.x, a.y, b.x, b.y, vr.h, vr.l);
             df_fma(a.z, a.w, b.z, b.w, vr.h, vr.l);
         }
         if (im)
         {
-            vi = DFv{0.f, 0.f};
-            df_fma(a.x, a.y, b.z, b.w, vi.h, vi.l);
+            df_mul(a.x, a.y, b.z, b.w, vi.h, vi.l);
             df_fma(-a.z, -a.w, b.x, b.y, vi.h, vi.l);
         }
     }
+    // four levels of butterflies without renormalising (each value's low
+    // part absorbs four exact errors), renormalised once as a cell
     static __device__ __forceinline__ void butterfly(val &a, val &b)
     {
         DFv s = a, d = a;
-        df_add(s.h, s.l, b.h, b.l);
-        df_add(d.h, d.l, -b.h, -b.l);
+        df_add_lazy(s.h, s.l, b.h, b.l);
+        df_add_lazy(d.h, d.l, -b.h, -b.l);
         a = s;
         b = d;
     }
     static __device__ __forceinline__ cell to_cell(val v)
     {
+        df_norm(v.h, v.l);
         return make_float2(v.h, v.l);
     }
     static __device__ __forceinline__ void add_cell(val &s, cell c, bool neg)
