@@ -25,6 +25,8 @@
 // from the split copy of the state (k_df_split), running df64 sums,
 // float64 across threads; a value outside the df64 range was flagged by
 // the split, and the pair kernel's float64 form recomputes the groups.
+#include <type_traits>
+
 #include "df64.cuh"
 #include "expect_body.cuh"
 
@@ -195,14 +197,17 @@ template <bool DF, int NS> constexpr int kTileMinBlocks = DF ? (NS == kTileSlots
 // DF: psi = the df64 split copy (float4 per element); else float2 elements.
 // NS = 6: one CTA per unit; NS = 3: two CTAs per unit (blockIdx.x = 2 unit +
 // half), each with half the slots and half the accumulator registers.
-template <bool DF, int NS>
+// OFF32: 2^n x S < 2^31, so that the tile rows' offsets from the tile's
+// first row fit 32 bits (one wide multiply-add per row load)
+template <bool DF, int NS, bool OFF32>
 __global__ void __launch_bounds__(256, kTileMinBlocks<DF, NS>)
     k_expect_tile(const void *__restrict__ psi, int64_t S, int n, const StringRec *__restrict__ recs,
                   const int32_t *__restrict__ orig, int64_t P, const TileChunk *__restrict__ units, int TC,
                   int n_splits, double *__restrict__ out)
 {
     extern __shared__ double red[]; // 256 * 4 * NS float pairs, then TC * 4 * NS doubles
-    __shared__ int64_t s_off[16];
+    using Off = std::conditional_t<OFF32, int32_t, int64_t>;
+    __shared__ Off s_off[16];
     const TileChunk u = units[NS == kTileSlots ? blockIdx.x : blockIdx.x >> 1];
     const int sb = NS == kTileSlots ? 0 : (int)(blockIdx.x & 1) * NS; // first slot of this CTA
     int act = 0;
@@ -219,7 +224,7 @@ __global__ void __launch_bounds__(256, kTileMinBlocks<DF, NS>)
     const bool col_ok = t0 < S;
     const int q0 = u.q[0], q1 = u.q[1], q2 = u.q[2], q3 = u.q[3];
     if (tid < 16)
-        s_off[tid] = (int64_t)(((uint64_t)(tid & 1) << q0) | ((uint64_t)((tid >> 1) & 1) << q1) |
+        s_off[tid] = (Off)(((uint64_t)(tid & 1) << q0) | ((uint64_t)((tid >> 1) & 1) << q1) |
                                ((uint64_t)((tid >> 2) & 1) << q2) | ((uint64_t)((tid >> 3) & 1) << q3)) *
                      S;
     __syncthreads();
@@ -243,13 +248,15 @@ __global__ void __launch_bounds__(256, kTileMinBlocks<DF, NS>)
             base = ((base >> q2) << (q2 + 1)) | (base & ((1ull << q2) - 1ull));
             base = ((base >> q3) << (q3 + 1)) | (base & ((1ull << q3) - 1ull));
             const int64_t e0 = (int64_t)base * S + t0;
+            const float4 *row4 = reinterpret_cast<const float4 *>(psi) + e0;
+            const float2 *row2 = reinterpret_cast<const float2 *>(psi) + e0;
             if constexpr (DF)
             {
                 float rows[16][4];
 #pragma unroll
                 for (int t = 0; t < 16; ++t)
                 {
-                    const float4 v = __ldg(reinterpret_cast<const float4 *>(psi) + e0 + s_off[t]);
+                    const float4 v = __ldg(row4 + s_off[t]);
                     rows[t][0] = v.x;
                     rows[t][1] = v.y;
                     rows[t][2] = v.z;
@@ -269,7 +276,7 @@ __global__ void __launch_bounds__(256, kTileMinBlocks<DF, NS>)
 #pragma unroll
                 for (int t = 0; t < 16; ++t)
                 {
-                    const float2 v = __ldg(reinterpret_cast<const float2 *>(psi) + e0 + s_off[t]);
+                    const float2 v = __ldg(row2 + s_off[t]);
                     rows[t][0] = v.x;
                     rows[t][1] = v.y;
                 }
@@ -326,18 +333,30 @@ __global__ void __launch_bounds__(256, kTileMinBlocks<DF, NS>)
     }
 }
 
-template <bool DF, int NS>
+template <bool DF, int NS, bool OFF32>
 cudaError_t launch_tile(const void *psi, int64_t S, int n, const DevOp &op, const TileChunk *d_units, int n_units,
                         int TC, int n_ctiles, int n_splits, double *out, cudaStream_t st)
 {
     dim3 grid((unsigned)(n_units * (kTileSlots / NS)), (unsigned)n_splits, (unsigned)n_ctiles);
     // every thread's (hi, lo) pairs, then the column totals
     const size_t smem = (size_t)256 * 4 * NS * sizeof(float2) + (size_t)TC * 4 * NS * sizeof(double);
-    if (cudaError_t e = cudaFuncSetAttribute(k_expect_tile<DF, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem))
+    if (cudaError_t e = cudaFuncSetAttribute(k_expect_tile<DF, NS, OFF32>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))
         return e;
-    k_expect_tile<DF, NS><<<grid, 256, smem, st>>>(psi, S, n, op.recs, op.orig, op.P, d_units, TC, n_splits, out);
+    k_expect_tile<DF, NS, OFF32>
+        <<<grid, 256, smem, st>>>(psi, S, n, op.recs, op.orig, op.P, d_units, TC, n_splits, out);
     return launched();
+}
+
+template <bool DF, int NS>
+cudaError_t launch_tile(const void *psi, int64_t S, int n, const DevOp &op, const TileChunk *d_units, int n_units,
+                        int TC, int n_ctiles, int n_splits, double *out, cudaStream_t st)
+{
+    // float64 only: the step of the n=14 weight<=2 workload 2.92 -> 2.80 ms;
+    // the complex64 form measured 8.5 -> 8.8 ms at n=18 with it
+    if (DF && (((int64_t)1 << n) * S) < ((int64_t)1 << 31))
+        return launch_tile<DF, NS, true>(psi, S, n, op, d_units, n_units, TC, n_ctiles, n_splits, out, st);
+    return launch_tile<DF, NS, false>(psi, S, n, op, d_units, n_units, TC, n_ctiles, n_splits, out, st);
 }
 
 } // namespace
