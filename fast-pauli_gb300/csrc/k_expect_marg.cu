@@ -26,7 +26,10 @@
 //  * complex128 states: double-float (df64.cuh) throughout the block and
 //    across blocks -- the float64 result to ~2^-46 of sum |terms| at float32
 //    pipe rates -- and float64 across threads.
+#include <type_traits>
+
 #include "df64.cuh"
+
 #include "expect_body.cuh"
 
 namespace fpg
@@ -326,6 +329,11 @@ __device__ __forceinline__ void block_marginals(const typename A::in_t *__restri
         // before any of them is used (batches of the half's 16)
         constexpr int PF = A::kPrefetchRows > 0 ? A::kPrefetchRows : 1;
         typename A::raw_t ra[PF], rb[PF];
+        // the block's first rows of this column, when psi points at whole
+        // elements (the df64 split copy): row loads add r * S only
+        constexpr bool kElemPtr = std::is_same_v<typename A::in_t, typename A::raw_t>;
+        [[maybe_unused]] const typename A::in_t *pa = psi + ((int64_t)base * S + t0);
+        [[maybe_unused]] const typename A::in_t *pb = psi + ((int64_t)baseB * S + t0);
 #pragma unroll
         for (int k = 0; k < 4; ++k)
         {
@@ -342,8 +350,16 @@ __device__ __forceinline__ void block_marginals(const typename A::in_t *__restri
                         rb[j] = A::raw_zero();
                         if ((int)r < RB)
                         {
-                            ra[j] = A::ld(psi, (int64_t)(base + r) * S + t0);
-                            rb[j] = A::ld(psi, (int64_t)(baseB + (r ^ xl)) * S + t0);
+                            if constexpr (kElemPtr)
+                            {
+                                ra[j] = A::ld(pa, (int64_t)r * S);
+                                rb[j] = A::ld(pb, (int64_t)(r ^ xl) * S);
+                            }
+                            else
+                            {
+                                ra[j] = A::ld(psi, (int64_t)(base + r) * S + t0);
+                                rb[j] = A::ld(psi, (int64_t)(baseB + (r ^ xl)) * S + t0);
+                            }
                         }
                     }
                 }
