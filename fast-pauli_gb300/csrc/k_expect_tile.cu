@@ -20,11 +20,12 @@
 // Layout: TC column lanes (one complex element each) x TR = 256 / TC row
 // lanes; grid (units, row splits, column tiles), units fastest, so that
 // concurrent CTAs read the same column tile (sized to stay in L2).
-// float32: tile sums in float32, Kahan-compensated across tiles, float64
-// across threads.  float64: double-float (df64.cuh) on the float32 pipes
-// from the split copy of the state (k_df_split), running df64 sums,
-// float64 across threads; a value outside the df64 range was flagged by
-// the split, and the pair kernel's float64 form recomputes the groups.
+// float32: tile sums in float32, Kahan-compensated across tiles.  float64:
+// double-float (df64.cuh) on the float32 pipes from the split copy of the
+// state (k_df_split), running df64 sums; a value outside the df64 range was
+// flagged by the split, and the pair kernel's float64 form recomputes the
+// groups.  Both sum over the row lanes in double-float pairs and convert
+// only the column totals to float64.
 #include <type_traits>
 
 #include "df64.cuh"
@@ -354,8 +355,9 @@ cudaError_t launch_tile(const void *psi, int64_t S, int n, const DevOp &op, cons
 {
     // float64 only: the step of the n=14 weight<=2 workload 2.92 -> 2.80 ms;
     // the complex64 form measured 8.5 -> 8.8 ms at n=18 with it
-    if (DF && (((int64_t)1 << n) * S) < ((int64_t)1 << 31))
-        return launch_tile<DF, NS, true>(psi, S, n, op, d_units, n_units, TC, n_ctiles, n_splits, out, st);
+    if constexpr (DF)
+        if ((((int64_t)1 << n) * S) < ((int64_t)1 << 31))
+            return launch_tile<DF, NS, true>(psi, S, n, op, d_units, n_units, TC, n_ctiles, n_splits, out, st);
     return launch_tile<DF, NS, false>(psi, S, n, op, d_units, n_units, TC, n_ctiles, n_splits, out, st);
 }
 
