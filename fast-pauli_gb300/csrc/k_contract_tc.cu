@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(128, 1)
     uint64_t *empty = full + NSTAGE;
     uint64_t *done = empty + NSTAGE;
     uint32_t *tmem_slot = (uint32_t *)(done + 1);
-    int *status = (int *)(tmem_slot + 1); // producer's verdict, shared with the epilogue
+    int *status = (int *)(tmem_slot + 1); // the producer's status, read by the epilogue
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t mt = blockIdx.y, nt = blockIdx.x;
