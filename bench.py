@@ -13,16 +13,25 @@ Under torchrun (N > 1) every rank runs its own full workload on its own GPU
 Rank 0 prints one JSON line.
 
 Keys beyond the base contract:
-  roofline      streaming-equivalent bytes (16 B per amplitude-term + coeffs +
-                outputs) of the dominant stage (the per-string expectation
-                kernels, timed alone with CUDA events) vs the measured HBM copy
-                bandwidth; "pipe" gives the same stage's float64 operation rate
-                vs the measured float64 FMA peak.
-  cpu_baseline  the CPU oracle port (OpenMP, all host threads) on a bounded
-                sample of the same workload.
+  roofline      the dominant stage (the per-string expectation kernels,
+                fpg_expect_strings, timed alone with CUDA events on its
+                stream) against its binding roof: float32 FMA-pipe issue.  The
+                stage runs its float64 arithmetic as double-float on the
+                float32 pipes; achieved = the stage's float64 operations
+                (fpg_operator_stats: 4 multiply-adds per row visit plus the
+                sign additions) x the float32 instructions each costs in
+                double-float (12 per multiply-add, 8 per addition) / time;
+                peak = the float32 FMA rate measured on this GPU
+                (fpg_measure_peak).  "streaming_equiv" keeps the
+                streaming-equivalent HBM figure (16 B per amplitude-term), and
+                "dram_frac" the stage's real DRAM rate (ncu bytes / time).
+  cpu_baseline  the CPU oracle port (OpenMP, all host threads) on the whole
+                workload (all 861 strings), with the host CPU named.
+  e2e           the public API with host numpy states: pinned (value) and
+                ordinary pageable memory ("pageable").
   mixed         the complex64 / float32 path on the n = 18 shape (1431 strings,
                 K = 1000, 262144 x 512), its throughput and its error against
-                the float64 GPU path.
+                the float64 oracle on a column slice.
 """
 
 from __future__ import annotations
@@ -45,10 +54,28 @@ for _p in (ROOT, PKG):
 
 METRIC = "expval amplitude-terms/s"
 UNIT = "amplitude-terms/s"
-# float64 FMA throughput of a GB300 measured on this machine with an independent
-# FMA-chain kernel (1.19 TFLOP/s, FMA = 2 FLOP); MEASURED_PEAKS.json has no
-# float64 figure.
-FP64_PEAK_TFLOPS = 1.19
+# float32 FMA-pipe instructions of one double-float operation (df64.cuh):
+# a multiply-add (df_fma: 1 multiply, 3 fused multiply-adds, 8 additions) and
+# an addition (df_add_lazy: TwoSum and two additions)
+DF64_FMA_OPS = 12
+DF64_ADD_OPS = 8
+
+
+def host_cpu() -> dict:
+    """Host CPU model, logical CPUs and the OpenMP thread setting."""
+    import platform
+
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.lower().startswith("model name"):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    return {"model": model or platform.processor() or platform.machine(), "arch": platform.machine(),
+            "nproc": os.cpu_count(), "OMP_NUM_THREADS": os.environ.get("OMP_NUM_THREADS")}
 
 
 def _peaks():
@@ -231,37 +258,46 @@ def run_ours(args, rank, world, dist):
     if rank != 0:
         return None
 
-    # result sanity: identity-free strings, Hermitian -> E has the symmetry
-    # E(h) real-linear; check a column against the oracle on a tiny slice
     hbm, peak_kind = _peaks()
-    e_bytes = 16
-    alg_bytes_expect = terms * e_bytes
+    fp32_rate = _abi.measure_peak(_abi.FPG_C64, stream)   # float32 FMA lane operations / s
+    fp64_rate = _abi.measure_peak(_abi.FPG_C128, stream)  # float64
     nch, visits, adds = op.stats()
-    fp64_ops = S * (4 * visits + adds)
+    fp64_ops = S * (4 * visits + adds)  # float64 multiply-adds and additions per stage
+    fp32_ops = S * (4 * visits * DF64_FMA_OPS + adds * DF64_ADD_OPS)
+    alg_bytes_expect = terms * 16
     traffic = _ncu_traffic("expect_stage_n14_weight2_fp64.md")
     roof = {
-        "bound": "hbm",
-        "achieved": alg_bytes_expect / t_expect / 1e9,
-        "peak": hbm,
-        "unit": "GB/s",
-        "frac": alg_bytes_expect / t_expect / 1e9 / hbm,
-        "peak_kind": peak_kind,
+        "bound": "fp32-issue",
+        "achieved": fp32_ops / t_expect / 1e12,
+        "peak": fp32_rate / 1e12,
+        "unit": "T float32 FMA-pipe lane-ops/s",
+        "frac": fp32_ops / t_expect / fp32_rate,
+        "peak_kind": "measured on this GPU (fpg_measure_peak: independent float32 FMA chains, all SMs)",
+        "kernel": "expectation stage (fpg_expect_strings: k_df_split + k_expect_tile + k_expect_marg + k_expect_wht "
+                  "+ family reductions)",
+        "kernel_ms": t_expect * 1e3,
+        "ops_per_launch": fp32_ops,
+        "model": "float64 operations of the stage (fpg_operator_stats: 4 multiply-adds per row visit + sign "
+                 "additions) x float32 instructions per double-float operation (12 per multiply-add, 8 per "
+                 "addition); an upper estimate (the marginal and transform kernels form each first product "
+                 "without an addition)",
         "traffic": traffic,
-        # the stage's real DRAM rate: ncu's DRAM bytes per stage over the
-        # CUDA-event stage time (the stage is bound by double-float issue, not
-        # by HBM)
+        "traffic_source": "ncu DRAM bytes of one stage launch, profiles/expect_stage_n14_weight2_fp64.md "
+                          "(captured once, not in this run)",
         "dram_achieved_gbs": traffic / t_expect / 1e9 if traffic else None,
         "dram_frac": traffic / t_expect / 1e9 / hbm if traffic else None,
-        "kernel": "expectation stage (fpg_expect_strings: k_df_split + k_expect_tile + k_expect_marg + k_expect_wht)",
-        "kernel_ms": t_expect * 1e3,
-        "algorithmic_bytes_per_launch": alg_bytes_expect,
-        "pipe": {"kind": "fp64-equivalent", "ops_per_launch": fp64_ops,
-                 "achieved_tflops": 2 * fp64_ops / t_expect / 1e12,
-                 "fp64_pipe_peak_tflops": FP64_PEAK_TFLOPS,
-                 "vs_fp64_pipe": 2 * fp64_ops / t_expect / 1e12 / FP64_PEAK_TFLOPS,
-                 "note": "the stage's float64 operations (FMA-equivalent x2) per second, against the measured float64 "
-                         "pipe; above 1 because the kernels run the float64 arithmetic as double-float on the "
-                         "float32 pipes"},
+        "hbm_peak_gbs": hbm,
+        "hbm_peak_kind": peak_kind,
+        "streaming_equiv": {"bytes_per_launch": alg_bytes_expect, "achieved_gbs": alg_bytes_expect / t_expect / 1e9,
+                            "vs_hbm_peak": alg_bytes_expect / t_expect / 1e9 / hbm,
+                            "note": "16 B per amplitude-term, the traffic of the reference's per-string streaming; "
+                                    "above 1 because the kernels read each amplitude once per kernel family, not "
+                                    "once per string"},
+        "fp64_pipe": {"ops_per_launch": fp64_ops, "achieved_tflops": 2 * fp64_ops / t_expect / 1e12,
+                      "peak_tflops": 2 * fp64_rate / 1e12,
+                      "vs_peak": fp64_ops / t_expect / fp64_rate,
+                      "note": "the stage's float64 operations per second against the float64 pipe measured on this "
+                              "GPU; above 1 because they run as double-float on the float32 pipes"},
     }
 
     # ---- end to end through the public API, host (pinned) buffers ---------
@@ -285,6 +321,19 @@ def run_ours(args, rank, world, dist):
                "overlap": "two column chunks, the first a quarter of the states: the rest is copied in while the "
                           "first is computed",
                "max_rel_err_vs_device_path": e2e_err}
+        # the same call with an ordinary (pageable) numpy array, as a drop-in
+        # user of the reference passes it
+        pageable = np.array(host, copy=True)
+        res = sop.expectation_value(pageable)
+        t0 = time.perf_counter()
+        for _ in range(ksteps):
+            res = sop.expectation_value(pageable)
+        t1 = time.perf_counter()
+        e2e["pageable"] = {"value": world * terms / ((t1 - t0) / ksteps), "unit": UNIT,
+                           "ms_per_call": (t1 - t0) / ksteps * 1e3,
+                           "api": "fast_pauli.SummedPauliOp.expectation_value(numpy, pageable host memory)",
+                           "max_rel_err_vs_device_path": float(np.abs(res - ref_dev).max() / np.abs(ref_dev).max())}
+        del pageable
 
     # ---- CPU baseline (oracle port, bounded sample) ------------------------
     cpu = None
@@ -311,22 +360,20 @@ def run_ours(args, rank, world, dist):
 
 
 def cpu_sample(strings, h, psi, S, n):
-    """Oracle port (the reference's OpenMP algorithm) on a bounded sample:
-    the first 108 of the 861 strings (1/8), all K and all states."""
-    import numpy as np
-
+    """Oracle port (the reference's OpenMP algorithm, all host threads) on the
+    whole workload: all 861 strings, K = 1000, all states, one call."""
     import oracle
 
-    sub = 108
-    hs = np.ascontiguousarray(h[:sub])
     host = psi.cpu().numpy()
-    oracle.summed_expectation(strings[:2], hs[:2], host[:, :8])  # load + warm
+    oracle.summed_expectation(strings[:2], h[:2], host[:, :8])  # load + warm
     t0 = time.perf_counter()
-    oracle.summed_expectation(strings[:sub], hs, host)
+    oracle.summed_expectation(strings, h, host)
     t = time.perf_counter() - t0
-    terms = sub * (1 << n) * S
+    terms = len(strings) * (1 << n) * S
     return {"value": terms / t, "unit": UNIT, "cores": oracle.max_threads(), "kind": "port",
-            "sample": f"first {sub} of 861 strings, K=1000, all 16384x1024 states ({t:.2f} s)"}
+            "host_cpu": host_cpu(),
+            "sample": f"the whole workload: all {len(strings)} strings, K={h.shape[1]}, all {1 << n}x{S} states, "
+                      f"one call ({t:.2f} s)"}
 
 
 def run_profile_c64(args):
@@ -365,10 +412,13 @@ def run_profile_c64(args):
 
 
 def run_mixed(args):
-    """complex64 / float32 path on the n=18 shape; error vs the float64 GPU path."""
+    """complex64 / float32 path on the n=18 shape: throughput, speed-up over
+    the float64 GPU path, and the error against the float64 oracle (on the
+    float64 states, before their conversion) over a slice of the columns."""
     import numpy as np
     import torch
 
+    import oracle
     from fast_pauli import _abi
 
     n, K, S = 18, 1000, 512
@@ -400,15 +450,27 @@ def run_mixed(args):
     got = out64.cpu().numpy().astype(np.complex128)
     err = np.abs(got - ref)
     den = np.abs(ref).max()
+    # the float64 oracle on 32 columns (first 16, last 16)
+    cols = np.r_[0:16, S - 16:S]
+    psi_slice = psi[:, torch.from_numpy(cols).cuda()].cpu().numpy()
     terms = P * D * S
     del psi, psi64
     torch.cuda.empty_cache()
+    t0 = time.perf_counter()
+    want = oracle.summed_expectation(strings, h, psi_slice)
+    t_or = time.perf_counter() - t0
+    got_s = got[:, cols]
+    err_o = np.abs(got_s - want)
     hbm, _ = _peaks()
     return {"workload": f"n={n}, {P} strings, K={K}, states {D}x{S} complex64", "terms_per_s": terms / t64,
             "ms_per_step": t64 * 1e3, "fp64_ms_per_step": t128 * 1e3, "speedup_vs_fp64": t128 / t64,
             "streaming_equiv_frac_of_hbm": terms * 8 / t64 / 1e9 / hbm,
-            "max_normwise_rel_err_vs_fp64": float(err.max() / den),
-            "mean_rel_err_vs_fp64": float(err.mean() / np.abs(ref).mean())}
+            "max_normwise_rel_err_vs_oracle": float(err_o.max() / np.abs(want).max()),
+            "mean_rel_err_vs_oracle": float(err_o.mean() / np.abs(want).mean()),
+            "oracle_sample": f"float64 oracle (C/OpenMP port) on {len(cols)} of {S} columns, all strings and "
+                             f"operators ({t_or:.1f} s)",
+            "max_normwise_rel_err_vs_fp64_gpu": float(err.max() / den),
+            "mean_rel_err_vs_fp64_gpu": float(err.mean() / np.abs(ref).mean())}
 
 
 def _ncu_traffic(summary: str):
@@ -426,8 +488,9 @@ def _ncu_traffic(summary: str):
 
 def run_reference(args, rank, world):
     """The reference's own CPU algorithm (oracle/_ref when built from the
-    reference sources on this machine, else the C restatement of it) on a
-    bounded sample of the same workload, all host threads."""
+    reference sources on this machine, else the C restatement of it) on the
+    whole workload every step (all 861 strings, K = 1000, 16384 x 1024
+    states), all host threads."""
     if rank != 0:
         return None
     import numpy as np
@@ -436,7 +499,6 @@ def run_reference(args, rank, world):
     from oracle import ref as oref
 
     n, K, S = 14, 1000, 1024
-    sub = 54  # strings per step (1/16 of 861): bounded sample
     rng = np.random.default_rng(1002)
     strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
     P = len(strings)
@@ -445,22 +507,24 @@ def run_reference(args, rank, world):
     use_ref = oref.available()
     fn = oref.summed_expectation if use_ref else oracle.summed_expectation
     for _ in range(args.warmup):
-        fn(strings[:sub], h[:sub], psi)
+        fn(strings, h, psi)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        fn(strings[:sub], h[:sub], psi)
+        fn(strings, h, psi)
     t = (time.perf_counter() - t0) / args.steps
-    terms = sub * (1 << n) * S
+    terms = P * (1 << n) * S
     v = terms / t
     kind = "reference" if use_ref else "port"
+    cpu = host_cpu()
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128/f64", "data": "synthetic",
             "config": {"workload": "SummedPauliOp.expectation_value float64: n=14, 861 weight<=2 strings, "
                                    "K=1000, states 16384x1024 complex128",
-                       "sample_per_step": f"{sub} of {P} strings, K=1000, all states"},
+                       "sample_per_step": "the whole workload (all strings, operators and states)"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": oracle.max_threads(), "kind": kind,
-                             "sample": f"{sub} of {P} strings per step"},
+                             "host_cpu": cpu,
+                             "sample": f"all {P} strings, K={K}, all states, every step"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 

@@ -29,7 +29,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["k_expect.cu", "k_expect_wht.cu", "k_apply.cu", "k_contract.cu", "k_contract_tc.cu", "k_noalloc.cu",
-              "batch.cu", "k_expect_pair.cu", "k_expect_tile.cu", "k_expect_marg.cu", "k_square.cu", "k_product.cu", "k_df64.cu"]
+              "batch.cu", "k_expect_pair.cu", "k_expect_tile.cu", "k_expect_marg.cu", "k_square.cu", "k_product.cu", "k_df64.cu",
+              "k_peak.cu"]
 CPP_SOURCES = ["capi.cpp", "server.cpp"]
 
 

@@ -35,6 +35,21 @@ cudaError_t launched()
     g_launches.fetch_add(1, std::memory_order_relaxed);
     return cudaGetLastError();
 }
+int sm_count()
+{
+    constexpr int kMaxDev = 64;
+    static std::atomic<int> cache[kMaxDev] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev)
+        return 152;
+    int v = cache[dev].load(std::memory_order_relaxed);
+    if (v > 0)
+        return v;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+        return 152;
+    cache[dev].store(v, std::memory_order_relaxed);
+    return v;
+}
 int set_error(int code, const std::string &msg)
 {
     g_last_error = msg;
@@ -544,7 +559,7 @@ ExpectPlan plan_expect(const fpg_operator *op, int64_t S, bool fp32, const void 
     auto pick = [](int64_t ctas_per_split, int64_t blocks, int row_lanes, bool windowed, int64_t window) {
         if (ctas_per_split <= 0)
             return 1;
-        const int64_t target = 152 * 8;
+        const int64_t target = (int64_t)sm_count() * 8;
         int64_t s = (target + ctas_per_split - 1) / ctas_per_split;
         if (windowed)
             s = std::max<int64_t>(s, (blocks + window - 1) / window);

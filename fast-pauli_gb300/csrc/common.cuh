@@ -127,6 +127,10 @@ struct DevOp
 // ---------------------------------------------------------------------------
 cudaError_t launched();
 
+// Multiprocessor count of the current device (cached per device ordinal;
+// 152 on a GB300).  Grid sizes are multiples of it.
+int sm_count();
+
 // Chunk classes of the expectation kernel: (max even strings, max odd strings).
 constexpr int kNumChunkClasses = 8;
 struct ChunkClass

@@ -352,8 +352,8 @@ cudaError_t launch_prep_weighted(bool fp32, const DevOp &op, const void *W, int6
     if (op.P <= 0 || S <= 0)
         return cudaSuccess;
     int64_t blocks = (op.P * S + 255) / 256;
-    if (blocks > 152 * 16)
-        blocks = 152 * 16;
+    if (blocks > (int64_t)sm_count() * 16)
+        blocks = (int64_t)sm_count() * 16;
     const unsigned grid = (unsigned)blocks;
     if (fp32)
         k_prep_weighted<float2><<<grid, 256, 0, st>>>(op.recs, op.orig, op.P, (const float2 *)W, S, (float2 *)cw);
@@ -432,8 +432,8 @@ cudaError_t launch_to_tensor(bool fp32, const DevOp &op, const void *coeffs, int
         return cudaSuccess;
     const uint64_t total = (uint64_t)K * (1ull << op.n) * (uint64_t)op.G;
     uint64_t blocks = (total + 255) / 256;
-    if (blocks > 152 * 32)
-        blocks = 152 * 32;
+    if (blocks > (int64_t)sm_count() * 32)
+        blocks = (int64_t)sm_count() * 32;
     if (fp32)
         k_to_tensor<float2><<<(unsigned)blocks, 256, 0, st>>>(op.recs, op.orig, op.groups, op.G,
                                                               (const float2 *)coeffs, K, op.n, (float2 *)out);
@@ -447,8 +447,8 @@ cudaError_t launch_sparse_repr(uint64_t x, uint64_t z, int ny, int n, uint64_t *
 {
     const uint64_t D = 1ull << n;
     uint64_t blocks = (D + 255) / 256;
-    if (blocks > 152 * 32)
-        blocks = 152 * 32;
+    if (blocks > (int64_t)sm_count() * 32)
+        blocks = (int64_t)sm_count() * 32;
     k_sparse_repr<<<(unsigned)blocks, 256, 0, st>>>(x, z, ny, D, cols, (double2 *)vals);
     return launched();
 }

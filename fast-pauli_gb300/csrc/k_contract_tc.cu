@@ -399,7 +399,8 @@ int64_t round_up(int64_t v, int64_t m)
 unsigned grid_for(int64_t n)
 {
     int64_t b = (n + 255) / 256;
-    return (unsigned)(b < 1 ? 1 : (b > 152 * 16 ? 152 * 16 : b));
+    const int64_t cap = (int64_t)sm_count() * 16;
+    return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 
 // 32-deep chunks per float32 accumulation segment: one chunk (12 MMAs of

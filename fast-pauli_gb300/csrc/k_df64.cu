@@ -32,8 +32,8 @@ cudaError_t launch_df_split(const void *psi, int64_t count, void *out, int *rang
     if (count <= 0)
         return cudaSuccess;
     int64_t blocks = (count + 255) / 256;
-    if (blocks > 152 * 16)
-        blocks = 152 * 16;
+    if (blocks > (int64_t)sm_count() * 16)
+        blocks = (int64_t)sm_count() * 16;
     k_df_split<<<(unsigned)blocks, 256, 0, st>>>((const uint4 *)psi, count, (float4 *)out, range_flag);
     return launched();
 }

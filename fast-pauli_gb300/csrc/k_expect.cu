@@ -125,8 +125,8 @@ cudaError_t launch_reduce_family(const double *partial, int n_splits, int64_t Pf
     if (count <= 0)
         return cudaSuccess;
     int64_t blocks = (count + 255) / 256;
-    if (blocks > 152 * 16)
-        blocks = 152 * 16;
+    if (blocks > (int64_t)sm_count() * 16)
+        blocks = (int64_t)sm_count() * 16;
     k_reduce_family<<<(unsigned)blocks, 256, 0, st>>>(partial, n_splits, Pf, S, glob, ev);
     return launched();
 }

@@ -328,7 +328,8 @@ __global__ void k_prod_reduce(const int32_t *__restrict__ idx, const int32_t *__
 unsigned grid_of(int64_t n, int threads)
 {
     int64_t b = (n + threads - 1) / threads;
-    return (unsigned)(b < 1 ? 1 : (b > 152 * 32 ? 152 * 32 : b));
+    const int64_t cap = (int64_t)sm_count() * 32;
+    return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 
 size_t al256(size_t b)

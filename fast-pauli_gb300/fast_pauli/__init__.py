@@ -16,17 +16,4 @@ from ._fast_pauli import (  # noqa: F401
     helpers,
     release_cached_memory,
 )
-
-
-def from_qiskit(*args, **kwargs):  # pragma: no cover - qiskit is not installed here
-    """qiskit interop (reference: fast_pauli/qiskit_helpers.py); needs qiskit."""
-    from .qiskit_helpers import from_qiskit as _f
-
-    return _f(*args, **kwargs)
-
-
-def to_qiskit(*args, **kwargs):  # pragma: no cover
-    """qiskit interop (reference: fast_pauli/qiskit_helpers.py); needs qiskit."""
-    from .qiskit_helpers import to_qiskit as _f
-
-    return _f(*args, **kwargs)
+from .qiskit_helpers import from_qiskit, to_qiskit  # noqa: F401  (qiskit itself is imported on use)

@@ -39,6 +39,7 @@ SIGNATURES = {
     "fpg_last_error": (ctypes.c_char_p, []),
     "fpg_kernel_launches": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint64)]),
     "fpg_device_error": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), _P]),
+    "fpg_measure_peak": (ctypes.c_int, [_I32, ctypes.POINTER(ctypes.c_double), _P]),
     "fpg_device_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int)]),
     "fpg_pointer_is_device": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
     "fpg_device_alloc": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_size_t, _P]),
@@ -140,6 +141,14 @@ def kernel_launches() -> int:
     v = ctypes.c_uint64()
     check(lib().fpg_kernel_launches(ctypes.byref(v)))
     return int(v.value)
+
+
+def measure_peak(dtype: int, stream=None) -> float:
+    """Measured FMA lane operations per second of the current device:
+    FPG_C64 = the float32 pipe, FPG_C128 = the float64 pipe."""
+    v = ctypes.c_double()
+    check(lib().fpg_measure_peak(dtype, ctypes.byref(v), stream))
+    return float(v.value)
 
 
 def check(rc: int) -> None:

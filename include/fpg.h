@@ -79,6 +79,14 @@ int fpg_kernel_launches(uint64_t *total);
  * invalid).  Synchronises `stream` and clears the flag. */
 int fpg_device_error(int *code, void *stream);
 
+/* Measured fused multiply-add rate of the current device, lane operations
+ * per second (one FMA = 1; multiply by 2 for FLOP/s): dtype FPG_C64 the
+ * float32 pipe, FPG_C128 the float64 pipe.  Runs a ~10 ms kernel of
+ * independent FMA chains on `stream` and synchronises it.  The roof of the
+ * float64 expectation stage, which runs as double-float on the float32
+ * pipes.  No reference counterpart (used to report rooflines). */
+int fpg_measure_peak(int32_t dtype, double *fma_per_s, void *stream);
+
 /* Number of visible CUDA devices (0 on a machine without a GPU). */
 int fpg_device_count(int *count);
 

@@ -5,6 +5,8 @@
 # copy bundled in torch/include, header-only), CCCL's cuda::std::mdspan (CUDA
 # toolkit) and the small shim in oracle/shim.  The reference's CMake cannot run
 # offline (it fetches its dependencies), so it is not used.
+# The reference tree is FP_REFERENCE_ROOT, by default the checkout this recipe
+# was written against; where it is absent the recipe builds nothing.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
 REF="${FP_REFERENCE_ROOT:-/root/reference}"

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 import oracle
-from conftest import TOL_C128, TOL_MIXED, golden, normwise
+from conftest import TOL_C128, TOL_MIXED, TOL_MIXED_W2, golden, normwise
 
 pytestmark = pytest.mark.gpu
 
@@ -172,7 +172,7 @@ def test_two_position_groups_tile_and_pair_kernels(case, n, S, c64):
     want = oracle.summed_expectation(strings, h, psi)
     states = torch.from_numpy(psi).to(torch.complex64 if c64 else torch.complex128).cuda()
     got = fp.SummedPauliOp(strings, h).expectation_value(states).cpu().numpy()
-    assert normwise(got, want) < (TOL_MIXED if c64 else TOL_C128)
+    assert normwise(got, want) < (TOL_MIXED_W2 if c64 else TOL_C128)
 
 
 @pytest.mark.parametrize("kind", ["weight2", "uniform", "weight2_c64", "weight2_tiny"])
@@ -197,7 +197,7 @@ def test_pinned_host_states(kind):
     t = torch.empty(psi.shape, dtype=dt, pin_memory=True)
     t.copy_(torch.from_numpy(psi))
     got = fp.SummedPauliOp(strings, h).expectation_value(t.numpy())
-    tol = TOL_MIXED if kind == "weight2_c64" else TOL_C128
+    tol = TOL_MIXED_W2 if kind == "weight2_c64" else TOL_C128
     assert normwise(got, want) < tol
 
 
@@ -223,7 +223,7 @@ def test_pinned_host_states_in_column_chunks(monkeypatch, chunks, S, c64):
     monkeypatch.setenv("FPG_HOST_CHUNKS", str(chunks))
     got = sop.expectation_value(t.numpy())
     assert got.shape == (K, S)
-    tol = TOL_MIXED if c64 else TOL_C128
+    tol = TOL_MIXED_W2 if c64 else TOL_C128
     assert normwise(got, want) < tol
     assert normwise(got, whole) < tol
 
@@ -589,7 +589,7 @@ def test_torch_device_tensors_c128_and_mixed():
     t64 = t128.to(torch.complex64)
     got64 = sop.expectation_value(t64)
     assert got64.dtype == torch.complex64
-    assert normwise(got64.cpu().numpy(), want) < TOL_MIXED
+    assert normwise(got64.cpu().numpy(), want) < TOL_MIXED_W2
     # apply on device, both precisions
     wa = oracle.summed_apply(strings, h, psi)
     assert normwise(sop.apply(t128).cpu().numpy(), wa) < TOL_C128
@@ -627,7 +627,11 @@ def test_tensor_core_contraction_3xtf32(K, S, n):
     assert code.value == 0
     want = h64.cpu().numpy().astype(np.complex128).T @ ev.cpu().numpy()
     assert normwise(out.cpu().numpy(), want) < 2e-6  # 3xTF32 with float32 accumulation
-    assert normwise(out.cpu().numpy(), oracle.summed_expectation(strings, h, psi)) < TOL_MIXED
+    # a single output (K = S = 1) is one cancelling sum of 36 terms: its
+    # relative error is the complex64 rounding of the terms times the
+    # cancellation ratio, so it is held to the looser bound
+    tol = TOL_MIXED if K * S == 1 else TOL_MIXED_W2
+    assert normwise(out.cpu().numpy(), oracle.summed_expectation(strings, h, psi)) < tol
     op.close()
 
 
