@@ -300,40 +300,41 @@ def run_ours(args, rank, world, dist):
                               "GPU; above 1 because they run as double-float on the float32 pipes"},
     }
 
-    # ---- end to end through the public API, host (pinned) buffers ---------
+    # ---- end to end through the public API, host numpy buffers -----------
+    # value: an ordinary (pageable) numpy array, as a drop-in user of the
+    # reference passes it; "pinned": the same call on page-locked memory
     e2e = None
     if not args.skip_e2e:
         sop = fp.SummedPauliOp(strings, h)
         pinned = torch.empty((D, S), dtype=torch.complex128, pin_memory=True)
         pinned.copy_(psi.cpu())
-        host = pinned.numpy()
-        res = sop.expectation_value(host)  # warm-up (encodes the strings once)
+        host_pinned = pinned.numpy()
+        host_pageable = np.array(host_pinned, copy=True)
         ref_dev = out.cpu().numpy()
-        e2e_err = float(np.abs(res - ref_dev).max() / np.abs(ref_dev).max())
         ksteps = max(3, args.steps // 2)
-        t0 = time.perf_counter()
-        for _ in range(ksteps):
-            res = sop.expectation_value(host)
-        t1 = time.perf_counter()
-        e2e = {"value": world * terms / ((t1 - t0) / ksteps), "unit": UNIT,
+
+        def e2e_time(host):
+            for _ in range(max(3, args.warmup)):  # warm-up (encoding cached, pool buffers mapped)
+                res = sop.expectation_value(host)
+            t0 = time.perf_counter()
+            for _ in range(ksteps):
+                res = sop.expectation_value(host)
+            t = (time.perf_counter() - t0) / ksteps
+            return t, float(np.abs(res - ref_dev).max() / np.abs(ref_dev).max())
+
+        t_pg, err_pg = e2e_time(host_pageable)
+        t_pn, err_pn = e2e_time(host_pinned)
+        e2e = {"value": world * terms / t_pg, "unit": UNIT,
                "h2d_bytes_per_step": D * S * 16 + P * K * 16, "d2h_bytes_per_step": K * S * 16,
-               "api": "fast_pauli.SummedPauliOp.expectation_value(numpy, pinned host memory)",
+               "ms_per_call": t_pg * 1e3,
+               "api": "fast_pauli.SummedPauliOp.expectation_value(numpy array in ordinary pageable host memory)",
                "overlap": "two column chunks, the first a quarter of the states: the rest is copied in while the "
                           "first is computed",
-               "max_rel_err_vs_device_path": e2e_err}
-        # the same call with an ordinary (pageable) numpy array, as a drop-in
-        # user of the reference passes it
-        pageable = np.array(host, copy=True)
-        res = sop.expectation_value(pageable)
-        t0 = time.perf_counter()
-        for _ in range(ksteps):
-            res = sop.expectation_value(pageable)
-        t1 = time.perf_counter()
-        e2e["pageable"] = {"value": world * terms / ((t1 - t0) / ksteps), "unit": UNIT,
-                           "ms_per_call": (t1 - t0) / ksteps * 1e3,
-                           "api": "fast_pauli.SummedPauliOp.expectation_value(numpy, pageable host memory)",
-                           "max_rel_err_vs_device_path": float(np.abs(res - ref_dev).max() / np.abs(ref_dev).max())}
-        del pageable
+               "max_rel_err_vs_device_path": err_pg,
+               "pinned": {"value": world * terms / t_pn, "unit": UNIT, "ms_per_call": t_pn * 1e3,
+                          "api": "fast_pauli.SummedPauliOp.expectation_value(numpy array in pinned host memory)",
+                          "max_rel_err_vs_device_path": err_pn}}
+        del host_pageable, pinned
 
     # ---- CPU baseline (oracle port, bounded sample) ------------------------
     cpu = None
@@ -343,6 +344,10 @@ def run_ours(args, rank, world, dist):
     mixed = None
     if not args.skip_mixed:
         mixed = run_mixed(args)
+
+    serve = None
+    if not args.skip_serve and world == 1:
+        serve = serve_summary()
 
     line = {
         "metric": METRIC, "value": world * terms / t_step, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -354,7 +359,7 @@ def run_ours(args, rank, world, dist):
                    "l2": "inputs (256 MiB states) larger than L2; no flush",
                    "parallelism": f"replicas x{world} (columns independent, no collective)"},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-        "launches_per_step": launches / args.steps, "clocks": clk, "mixed": mixed,
+        "launches_per_step": launches / args.steps, "clocks": clk, "mixed": mixed, "serve": serve,
     }
     return line
 
@@ -409,6 +414,41 @@ def run_profile_c64(args):
         _abi.check(L.fpg_summed_expect(op.handle, h64.data_ptr(), K, psi64.data_ptr(), out.data_ptr(), S,
                                        _abi.FPG_C64, stream))
     torch.cuda.synchronize()
+
+
+def run_profile_batch(args):
+    """One-shot case for launch lists: the 256 uneven problems as one batch
+    run (default tuning) and one pass of plain per-problem calls."""
+    import torch
+
+    from fast_pauli import _abi
+
+    torch.cuda.set_device(0)
+    L = _abi.lib()
+    stream = _stream_handle()
+    g = torch.Generator(device="cuda").manual_seed(4)
+    items = []
+    for n, strings, c, S in _cfg4_problems():
+        D = 1 << n
+        psi = torch.complex(torch.randn(D, S, device="cuda", generator=g),
+                            torch.randn(D, S, device="cuda", generator=g))
+        dc = torch.from_numpy(c.reshape(-1, 1)).to(torch.complex64).cuda()
+        items.append(dict(n=n, S=S, psi=psi, op=_abi.Operator(strings), c=dc,
+                          out=torch.zeros((1, S), dtype=torch.complex64, device="cuda")))
+    batch = _abi.Batch(_abi.FPG_C64)
+    for it in items:
+        batch.add(it["op"], it["c"].data_ptr(), 1, it["psi"].data_ptr(), it["out"].data_ptr(), it["S"])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    batch.run(stream)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for it in items:
+        _abi.check(L.fpg_summed_expect(it["op"].handle, it["c"].data_ptr(), 1, it["psi"].data_ptr(),
+                                       it["out"].data_ptr(), it["S"], _abi.FPG_C64, stream))
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    print(json.dumps({"batch_s": t1 - t0, "plain_s": t2 - t1}), flush=True)
 
 
 def run_mixed(args):
@@ -807,25 +847,21 @@ def normwise_np(got, want):
     return float(np.abs(got - want).max() / den) if den > 0 else float(np.abs(got - want).max())
 
 
-def run_serve(args):
-    """Serving: Poisson arrivals of expectation_value / apply_weighted
-    requests (n ~ U{10..max_n}, strings log-uniform 32..2048, S ~ U{1..64},
-    K log-uniform 1..64, complex64) against the serving loop (continuous
-    admission, 8 slots, HBM budget) and against the plain per-request path
-    (one slot, first come first served).  Latency = completion - arrival."""
+def _serve_requests(n_req, max_n, seed=1005):
+    """Poisson-mix requests (n ~ U{10..max_n}, strings log-uniform 32..2048,
+    S ~ U{1..64}, K log-uniform 1..64, 50/50 expectation_value /
+    apply_weighted, complex64), with resident operators and device arrays."""
     import numpy as np
     import torch
 
     import oracle
     from fast_pauli import _abi
 
-    torch.cuda.set_device(0)
-    rng = np.random.default_rng(1005)
+    rng = np.random.default_rng(seed)
     g = torch.Generator(device="cuda").manual_seed(5)
-    n_req = args.requests
     reqs = []
-    for i in range(n_req):
-        n = int(rng.integers(10, args.max_n + 1))
+    for _ in range(n_req):
+        n = int(rng.integers(10, max_n + 1))
         P = int(np.exp(rng.uniform(np.log(32), np.log(2048))))
         S = int(rng.integers(1, 65))
         K = int(np.exp(rng.uniform(0, np.log(64))))
@@ -841,44 +877,89 @@ def run_serve(args):
         reqs.append(dict(n=n, P=P, S=S, K=K, kind=kind, op=_abi.Operator(strings), psi=psi, h=h, data=data,
                          out=torch.empty(out_shape, dtype=torch.complex64, device="cuda")))
     torch.cuda.synchronize()
-    unit_gaps = rng.exponential(1.0, size=n_req)  # scaled by 1/rate per run
+    return reqs, rng.exponential(1.0, size=n_req)
 
-    def serve(n_slots, rate):
-        gaps = unit_gaps / rate
-        srv = _abi.Server(_abi.FPG_C64, n_slots=n_slots, hbm_budget_bytes=args.budget_gb << 30)
-        # warm-up: one small request
-        r0 = min(reqs, key=lambda r: r["P"] << r["n"])
-        srv.wait(srv.submit(r0["kind"], r0["op"], r0["h"].data_ptr(), r0["K"], r0["psi"].data_ptr(),
-                            r0["out"].data_ptr(), r0["S"], r0["data"].data_ptr()))
-        tickets = []
-        t0 = time.perf_counter()
-        arrive = t0
-        for r, gap in zip(reqs, gaps):
-            arrive += gap
-            while time.perf_counter() < arrive:
-                time.sleep(min(1e-4, max(0.0, arrive - time.perf_counter())))
-            tickets.append(srv.submit(r["kind"], r["op"], r["h"].data_ptr(), r["K"], r["psi"].data_ptr(),
-                                      r["out"].data_ptr(), r["S"], r["data"].data_ptr()))
-        infos = [srv.wait(t) for t in tickets]
-        wall = time.perf_counter() - t0
-        st = srv.stats()
-        srv.close()
-        lat = np.array([(i["done_us"] - i["submit_us"]) / 1e3 for i in infos])
-        return lat, wall, st
 
-    terms = sum(r["P"] * (1 << r["n"]) * r["S"] for r in reqs)
-    rates = [float(x) for x in args.rates.split(",")]
-    ns = np.array([r["n"] for r in reqs])
-    # service time of every request alone (one slot, one at a time): the floor
-    # under any latency
+def _serve_once(reqs, unit_gaps, n_slots, rate, budget_gb):
+    """Submit the requests at Poisson arrival times (unit_gaps / rate) to a
+    server with n_slots slots; latency = completion - arrival."""
+    import numpy as np
+
+    from fast_pauli import _abi
+
+    gaps = unit_gaps / rate
+    srv = _abi.Server(_abi.FPG_C64, n_slots=n_slots, hbm_budget_bytes=budget_gb << 30)
+    r0 = min(reqs, key=lambda r: r["P"] << r["n"])  # warm-up: one small request
+    srv.wait(srv.submit(r0["kind"], r0["op"], r0["h"].data_ptr(), r0["K"], r0["psi"].data_ptr(),
+                        r0["out"].data_ptr(), r0["S"], r0["data"].data_ptr()))
+    tickets = []
+    t0 = time.perf_counter()
+    arrive = t0
+    for r, gap in zip(reqs, gaps):
+        arrive += gap
+        while time.perf_counter() < arrive:
+            time.sleep(min(1e-4, max(0.0, arrive - time.perf_counter())))
+        tickets.append(srv.submit(r["kind"], r["op"], r["h"].data_ptr(), r["K"], r["psi"].data_ptr(),
+                                  r["out"].data_ptr(), r["S"], r["data"].data_ptr()))
+    infos = [srv.wait(t) for t in tickets]
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    lat = np.array([(i["done_us"] - i["submit_us"]) / 1e3 for i in infos])
+    return lat, wall, st
+
+
+def _service_alone(reqs, budget_gb):
+    """GPU service time of every request alone (one slot, one at a time)."""
+    import numpy as np
+
+    from fast_pauli import _abi
+
     alone = []
-    srv = _abi.Server(_abi.FPG_C64, n_slots=1, hbm_budget_bytes=args.budget_gb << 30)
+    srv = _abi.Server(_abi.FPG_C64, n_slots=1, hbm_budget_bytes=budget_gb << 30)
     for r in reqs:
         info = srv.wait(srv.submit(r["kind"], r["op"], r["h"].data_ptr(), r["K"], r["psi"].data_ptr(),
                                    r["out"].data_ptr(), r["S"], r["data"].data_ptr()))
         alone.append((info["done_us"] - info["start_us"]) / 1e3)
     srv.close()
-    alone = np.array(alone)
+    return np.array(alone)
+
+
+def _latency_row(lat, ns, alone, wall, terms, n_req, st, slots, target_ms=10.0):
+    import numpy as np
+
+    le20 = ns <= 20
+    feasible = le20 & (alone < target_ms)
+    buckets = {}
+    for lo, hi in ((10, 14), (15, 20), (21, 24)):
+        m = (ns >= lo) & (ns <= hi)
+        if m.any():
+            buckets[f"n{lo}-{hi}"] = {"count": int(m.sum()), "p50_ms": float(np.percentile(lat[m], 50)),
+                                      "p99_ms": float(np.percentile(lat[m], 99))}
+    return {"slots": slots, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "p99_ms_n_le_20": float(np.percentile(lat[le20], 99)) if le20.any() else None,
+            "p99_ms_n_le_20_alone_under_10ms": float(np.percentile(lat[feasible], 99)) if feasible.any() else None,
+            "count_n_le_20": int(le20.sum()), "count_n_le_20_alone_under_10ms": int(feasible.sum()),
+            "throughput_terms_per_s": terms / wall, "requests_per_s": n_req / wall, "wall_s": wall,
+            "by_n": buckets, "peak_running": st["peak_running"], "peak_reserved_gb": st["peak_reserved_bytes"] / 2**30}
+
+
+def run_serve(args):
+    """Serving: Poisson arrivals of expectation_value / apply_weighted
+    requests (n ~ U{10..max_n}, strings log-uniform 32..2048, S ~ U{1..64},
+    K log-uniform 1..64, complex64) against the serving loop (continuous
+    admission, 8 slots, HBM budget) and against the plain per-request path
+    (one slot, first come first served).  Latency = completion - arrival."""
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(0)
+    n_req = args.requests
+    reqs, unit_gaps = _serve_requests(n_req, args.max_n)
+    terms = sum(r["P"] * (1 << r["n"]) * r["S"] for r in reqs)
+    rates = [float(x) for x in args.rates.split(",")]
+    ns = np.array([r["n"] for r in reqs])
+    alone = _service_alone(reqs, args.budget_gb)
     le20 = ns <= 20
     out = {"metric": "serving latency ms / amplitude-terms/s",
            "workload": f"serving: {n_req} requests per rate, Poisson rates {rates}/s, n~U{{10..{args.max_n}}}, "
@@ -892,20 +973,39 @@ def run_serve(args):
     for rate in rates:
         row = {"rate_per_s": rate}
         for name, slots in (("served", args.slots), ("plain_per_request", 1)):
-            lat, wall, st = serve(slots, rate)
-            buckets = {}
-            for lo, hi in ((10, 14), (15, 20), (21, 24)):
-                m = (ns >= lo) & (ns <= hi)
-                if m.any():
-                    buckets[f"n{lo}-{hi}"] = {"count": int(m.sum()), "p50_ms": float(np.percentile(lat[m], 50)),
-                                              "p99_ms": float(np.percentile(lat[m], 99))}
-            row[name] = {"slots": slots, "p50_ms": float(np.percentile(lat, 50)),
-                         "p99_ms": float(np.percentile(lat, 99)),
-                         "p99_ms_n_le_20": float(np.percentile(lat[le20], 99)),
-                         "throughput_terms_per_s": terms / wall, "requests_per_s": n_req / wall, "wall_s": wall,
-                         "by_n": buckets, "peak_running": st["peak_running"],
-                         "peak_reserved_gb": st["peak_reserved_bytes"] / 2**30}
+            lat, wall, st = _serve_once(reqs, unit_gaps, slots, rate, args.budget_gb)
+            row[name] = _latency_row(lat, ns, alone, wall, terms, n_req, st, slots)
         out["sweep"].append(row)
+    return out
+
+
+def serve_summary(n_req=40, rate=4.0, max_n=24, slots=8, budget_gb=64):
+    """Short serving run for the default line: one Poisson rate, the same
+    request mix as --workload serve, p50 / p99 overall and by qubit count,
+    and the p99 over the requests of n <= 20 whose GPU service time alone is
+    under 10 ms (the larger ones cannot meet a 10 ms target on one GPU: their
+    own work takes longer)."""
+    import numpy as np
+    import torch
+
+    reqs, unit_gaps = _serve_requests(n_req, max_n)
+    terms = sum(r["P"] * (1 << r["n"]) * r["S"] for r in reqs)
+    ns = np.array([r["n"] for r in reqs])
+    work = np.array([r["P"] * (1 << r["n"]) * r["S"] for r in reqs], dtype=np.float64)
+    alone = _service_alone(reqs, budget_gb)
+    lat, wall, st = _serve_once(reqs, unit_gaps, slots, rate, budget_gb)
+    row = _latency_row(lat, ns, alone, wall, terms, n_req, st, slots)
+    slow = (ns <= 20) & (alone >= 10.0)
+    out = {"workload": f"{n_req} requests, Poisson {rate}/s, n~U{{10..{max_n}}}, P log-uniform 32..2048 uniform "
+                       "strings, S~U{1..64}, K log-uniform 1..64, 50/50 expectation_value / apply_weighted, "
+                       "complex64, 8 slots",
+           "rate_per_s": rate, **row,
+           "service_alone_ms": {"p50": float(np.percentile(alone, 50)), "p99": float(np.percentile(alone, 99))},
+           "n_le_20_over_10ms_alone": {"count": int(slow.sum()),
+                                       "min_terms": float(work[slow].min()) if slow.any() else None,
+                                       "min_alone_ms": float(alone[slow].min()) if slow.any() else None}}
+    del reqs
+    torch.cuda.empty_cache()
     return out
 
 
@@ -915,13 +1015,16 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--profile", nargs="?", const="summed", default=None, choices=["summed", "mixed", "random"],
+    ap.add_argument("--profile", nargs="?", const="summed", default=None,
+                    choices=["summed", "mixed", "random", "batch"],
                     help="short device-only run for ncu captures: summed = the n=14 weight<=2 workload (float64), "
                          "mixed = the n=18 complex64 shape (tensor-core contraction), "
-                         "random = n=20, 1024 uniform random strings, 64 states, complex64")
+                         "random = n=20, 1024 uniform random strings, 64 states, complex64, "
+                         "batch = the 256 uneven problems: one batch run and one pass of plain calls")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-mixed", action="store_true")
+    ap.add_argument("--skip-serve", action="store_true")
     ap.add_argument("--workload", default="summed", choices=["summed", "batch", "serve", "square", "to_tensor", "product"],
                     help="summed: the n=14 weight<=2 SummedPauliOp workload (default line); batch: 256 uneven problems; "
                          "serve: the request loop; "
@@ -938,6 +1041,9 @@ def main():
     dist = None
     if args.profile in ("mixed", "random"):
         run_profile_c64(args)
+        return
+    if args.profile == "batch":
+        run_profile_batch(args)
         return
     if args.workload != "summed" and args.impl == "ours":
         if rank == 0:

@@ -1294,7 +1294,7 @@ template <std::floating_point T> struct SummedPauliOp
         fpg_operator *op = cache_.get(pauli_strings);
         cudaStream_t st = detail::stream();
         const size_t in_bytes = dim() * S * sizeof(C);
-        if (!detail::on_device(out) && detail::pinned_host(psi))
+        if (!detail::on_device(out) && !detail::on_device(psi))
             if (const size_t nc = detail::host_column_chunks(S, in_bytes); nc > 1)
                 return run_expect_overlapped(op, out, psi, S, out_zero, nc, st);
         detail::Staged in(psi, in_bytes, 0, st), o(out, n_operators() * S * sizeof(C), out_zero ? 2 : 1, st);
@@ -1308,11 +1308,15 @@ template <std::floating_point T> struct SummedPauliOp
   private:
     detail::EncodedCache cache_;
 
-    // Pinned host states in nc column chunks: every chunk's copy is queued at
-    // once on the thread's copy stream (the link runs them back to back), each
-    // chunk is computed on the call's stream as soon as its copy has landed,
-    // and the results are copied out after the last chunk.  Each chunk is an
-    // independent fpg_summed_expect call on its own columns.
+    // Host states in nc column chunks: chunk c's copy goes on the thread's
+    // copy stream (the link runs the copies back to back) and its computation
+    // on the call's stream, ordered after that copy, before chunk c + 1's
+    // copy is issued: from pinned memory the copies are asynchronous, and
+    // from pageable memory, whose copies return only once the host has handed
+    // the data over, chunk c is already running on the GPU while chunk
+    // c + 1 is being copied.  The results are copied out after the last
+    // chunk.  Each chunk is an independent fpg_summed_expect call on its own
+    // columns.
     template <typename C>
     void run_expect_overlapped(fpg_operator *op, C *out, const C *psi, size_t S, bool out_zero, size_t nc,
                                cudaStream_t st) const
@@ -1367,17 +1371,17 @@ template <std::floating_point T> struct SummedPauliOp
             detail::cuda_check(cudaMemcpy2DAsync(din[c].p, cw[c] * el, psi + c0[c], S * el, cw[c] * el, D,
                                                  cudaMemcpyHostToDevice, cs),
                                "cudaMemcpy2DAsync");
+            // an accumulating output is copied in on the copy stream too: a
+            // pageable copy on the call's stream would first wait for the
+            // chunks already running there
+            if (!out_zero)
+                detail::cuda_check(cudaMemcpy2DAsync(dout[c].p, cw[c] * el, out + c0[c], S * el, cw[c] * el, K,
+                                                     cudaMemcpyHostToDevice, cs),
+                                   "cudaMemcpy2DAsync");
             landed[c] = std::make_unique<detail::Event>();
             detail::cuda_check(cudaEventRecord(landed[c]->e, cs), "cudaEventRecord");
-        }
-        for (size_t c = 0; c < nc; ++c)
-        {
             if (out_zero)
                 detail::cuda_check(cudaMemsetAsync(dout[c].p, 0, dout[c].bytes, st), "cudaMemsetAsync");
-            else
-                detail::cuda_check(cudaMemcpy2DAsync(dout[c].p, cw[c] * el, out + c0[c], S * el, cw[c] * el, K,
-                                                     cudaMemcpyHostToDevice, st),
-                                   "cudaMemcpy2DAsync");
             detail::cuda_check(cudaStreamWaitEvent(st, landed[c]->e, 0), "cudaStreamWaitEvent");
             detail::check(fpg_summed_expect(op, dh.p, (int64_t)K, din[c].p, dout[c].p, (int64_t)cw[c],
                                             detail::dtype_of<C>(), st));

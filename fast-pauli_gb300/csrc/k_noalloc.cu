@@ -16,12 +16,22 @@
 // coefficients, states and the output.
 //
 // Set-up: the first call on each device resolves the array's device address
-// with cudaGetSymbolAddress (with that device current) and caches it; make
-// that first call before any stream capture begins, since resolving a symbol
-// may load the module.  All calls share the one array, so calls whose GPU
-// work overlaps (different streams, different host threads) race on it:
-// order them on one stream or synchronise between them.  The host-side
-// staging buffers are static too and are guarded by a mutex.
+// with cudaGetSymbolAddress (with that device current) and caches it for the
+// life of the process; a cudaDeviceReset invalidates that address, so the
+// entry point is not for processes that reset the device.  All calls share
+// the one array, so calls whose GPU work overlaps (different streams,
+// different host threads) race on it: order them on one stream or
+// synchronise between them.  The host-side staging arrays are static too and
+// are guarded by a mutex; the encoding is copied from them with pageable
+// copies, which have read their source when cudaMemcpyAsync returns.  A copy
+// recorded into a graph would instead read the arrays when the graph is
+// replayed, after later calls have overwritten them, so a call made while
+// its stream is being captured is refused (FPG_ERR_UNSUPPORTED).
+//
+// Work layout: one CTA per (chunk of up to 8 strings of an x-group, column
+// tile), rows not split, so an operator of only a few strings on a large
+// state (say under ten strings at n >= 24) runs on a few CTAs and is much
+// slower than fpg_summed_expect, which splits the rows into partial tables.
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -186,9 +196,18 @@ extern "C" int fpg_summed_expect_noalloc(const char *strings, int64_t n_strings,
                              " MiB static scratch (at most about " +
                              std::to_string(((int64_t)kNoallocScratchBytes - (int64_t)off_ev) / 8) + " values)");
 
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(st, &cap);
+    if (e != cudaSuccess)
+        return cuda_error(e, "cudaStreamIsCapturing");
+    if (cap != cudaStreamCaptureStatusNone)
+        return set_error(FPG_ERR_UNSUPPORTED, "fpg_summed_expect_noalloc: the stream is being captured; the encoding "
+                                              "is copied from host arrays that the next call overwrites");
+
     std::lock_guard<std::mutex> lock(g_mu);
     int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    e = cudaGetDevice(&dev);
     if (e != cudaSuccess)
         return cuda_error(e, "cudaGetDevice");
     if (dev < 0 || dev >= kMaxDevices)
@@ -209,7 +228,6 @@ extern "C" int fpg_summed_expect_noalloc(const char *strings, int64_t n_strings,
     if (int rc = encode_static(strings, P, n_qubits, &G, &C, class_begin))
         return rc;
 
-    cudaStream_t st = (cudaStream_t)stream;
     // pageable-source copies: each returns once the source has been staged,
     // so the static host arrays may be reused by the next call
     if ((e = cudaMemcpyAsync(base + off_recs, h_recs, (size_t)P * sizeof(StringRec), cudaMemcpyHostToDevice, st)) ||

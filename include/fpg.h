@@ -337,8 +337,13 @@ int fpg_server_destroy(fpg_server *server);
  * exit.
  * Limits: n_strings <= 8192 and n_strings * n_states up to about 2 million
  * (the table must fit the array); larger requests return FPG_ERR_INVALID.
- * The first call on a device resolves the array's address (make it before any
- * stream capture); calls whose GPU work overlaps race on the shared array.
+ * The first call on a device resolves the array's address and keeps it for
+ * the life of the process (so not for processes that call cudaDeviceReset);
+ * calls whose GPU work overlaps race on the shared array.  The encoding is
+ * copied from static host arrays, so a call made while `stream` is being
+ * captured returns FPG_ERR_UNSUPPORTED.  Rows are not split: an operator of
+ * a few strings on a large state runs on few CTAs (slower than
+ * fpg_summed_expect).
  * No counterpart in the reference.
  */
 int fpg_summed_expect_noalloc(const char *strings, int64_t n_strings, int32_t n_qubits, const void *coeffs,

@@ -201,12 +201,14 @@ def test_pinned_host_states(kind):
     assert normwise(got, want) < tol
 
 
+@pytest.mark.parametrize("pinned", [True, False])
 @pytest.mark.parametrize("chunks,S,c64", [(2, 128, False), (3, 300, False), (4, 257, True), (9, 200, False)])
-def test_pinned_host_states_in_column_chunks(monkeypatch, chunks, S, c64):
-    """Pinned host states of many columns are computed in column chunks, each
-    chunk's copy overlapping the previous chunk's computation: the results
-    (odd widths, more chunks asked for than 64-column pieces exist) match the
-    oracle and the one-call device path."""
+def test_pinned_host_states_in_column_chunks(monkeypatch, chunks, S, c64, pinned):
+    """Host states (pinned, or ordinary pageable numpy arrays) of many
+    columns are computed in column chunks, each chunk's copy overlapping the
+    previous chunk's computation: the results (odd widths, more chunks asked
+    for than 64-column pieces exist) match the oracle and the one-call device
+    path."""
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(chunks * 1000 + S)
     n, K = 8, 5
@@ -221,7 +223,7 @@ def test_pinned_host_states_in_column_chunks(monkeypatch, chunks, S, c64):
     sop = fp.SummedPauliOp(strings, h)
     whole = sop.expectation_value(t.cuda()).cpu().numpy()
     monkeypatch.setenv("FPG_HOST_CHUNKS", str(chunks))
-    got = sop.expectation_value(t.numpy())
+    got = sop.expectation_value(t.numpy() if pinned else np.array(t.numpy(), copy=True))
     assert got.shape == (K, S)
     tol = TOL_MIXED_W2 if c64 else TOL_C128
     assert normwise(got, want) < tol
