@@ -909,6 +909,53 @@ def _serve_once(reqs, unit_gaps, n_slots, rate, budget_gb):
     return lat, wall, st
 
 
+def _plain_once(reqs, unit_gaps, rate):
+    """The plain per-request path: each request's library call
+    (fpg_summed_expect or fpg_summed_apply_weighted, output zeroed first)
+    issued on one stream at its arrival, first come first served; completion
+    = its event on the stream, read as host time from an event recorded at
+    the start while the GPU was idle."""
+    import numpy as np
+    import torch
+
+    from fast_pauli import _abi
+
+    L = _abi.lib()
+    st = torch.cuda.current_stream()
+    handle = ctypes.c_void_p(st.cuda_stream)
+
+    def issue(r):
+        r["out"].zero_()
+        if r["kind"] == _abi.FPG_REQ_EXPECT:
+            _abi.check(L.fpg_summed_expect(r["op"].handle, r["h"].data_ptr(), r["K"], r["psi"].data_ptr(),
+                                           r["out"].data_ptr(), r["S"], _abi.FPG_C64, handle))
+        else:
+            _abi.check(L.fpg_summed_apply_weighted(r["op"].handle, r["h"].data_ptr(), r["K"], r["psi"].data_ptr(),
+                                                   r["data"].data_ptr(), r["out"].data_ptr(), r["S"], _abi.FPG_C64,
+                                                   handle))
+
+    issue(min(reqs, key=lambda r: r["P"] << r["n"]))  # warm-up
+    torch.cuda.synchronize()
+    gaps = unit_gaps / rate
+    e0 = torch.cuda.Event(enable_timing=True)
+    done = [torch.cuda.Event(enable_timing=True) for _ in reqs]
+    arrivals = []
+    t0 = time.perf_counter()
+    e0.record(st)
+    arrive = t0
+    for r, gap, ev in zip(reqs, gaps, done):
+        arrive += gap
+        while time.perf_counter() < arrive:
+            time.sleep(min(1e-4, max(0.0, arrive - time.perf_counter())))
+        arrivals.append(arrive - t0)
+        issue(r)
+        ev.record(st)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    lat = np.array([e0.elapsed_time(ev) - a * 1e3 for ev, a in zip(done, arrivals)])
+    return lat, wall
+
+
 def _service_alone(reqs, budget_gb):
     """GPU service time of every request alone (one slot, one at a time)."""
     import numpy as np
@@ -936,22 +983,29 @@ def _latency_row(lat, ns, alone, wall, terms, n_req, st, slots, target_ms=10.0):
         if m.any():
             buckets[f"n{lo}-{hi}"] = {"count": int(m.sum()), "p50_ms": float(np.percentile(lat[m], 50)),
                                       "p99_ms": float(np.percentile(lat[m], 99))}
-    return {"slots": slots, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "p99_ms_n_le_20": float(np.percentile(lat[le20], 99)) if le20.any() else None,
-            "p99_ms_n_le_20_alone_under_10ms": float(np.percentile(lat[feasible], 99)) if feasible.any() else None,
-            "count_n_le_20": int(le20.sum()), "count_n_le_20_alone_under_10ms": int(feasible.sum()),
-            "throughput_terms_per_s": terms / wall, "requests_per_s": n_req / wall, "wall_s": wall,
-            "by_n": buckets, "peak_running": st["peak_running"], "peak_reserved_gb": st["peak_reserved_bytes"] / 2**30}
+    row = {"slots": slots, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+           "p99_ms_n_le_20": float(np.percentile(lat[le20], 99)) if le20.any() else None,
+           "p99_ms_n_le_20_alone_under_10ms": float(np.percentile(lat[feasible], 99)) if feasible.any() else None,
+           "count_n_le_20": int(le20.sum()), "count_n_le_20_alone_under_10ms": int(feasible.sum()),
+           "throughput_terms_per_s": terms / wall, "requests_per_s": n_req / wall, "wall_s": wall, "by_n": buckets}
+    if st is not None:
+        row.update({"peak_running": st["peak_running"], "peak_reserved_gb": st["peak_reserved_bytes"] / 2**30,
+                    "merged_runs": st["merged_runs"], "merged_requests": st["merged_requests"]})
+    return row
 
 
 def run_serve(args):
     """Serving: Poisson arrivals of expectation_value / apply_weighted
     requests (n ~ U{10..max_n}, strings log-uniform 32..2048, S ~ U{1..64},
     K log-uniform 1..64, complex64) against the serving loop (continuous
-    admission, 8 slots, HBM budget) and against the plain per-request path
-    (one slot, first come first served).  Latency = completion - arrival."""
+    admission, 8 slots, HBM budget, small expectation requests merged) and
+    against the plain per-request path (each request's library call issued on
+    one stream at its arrival).  Latency = completion - arrival.  Then a
+    burst of small expectation requests at a high rate, both ways."""
     import numpy as np
     import torch
+
+    from fast_pauli import _abi
 
     torch.cuda.set_device(0)
     n_req = args.requests
@@ -972,10 +1026,28 @@ def run_serve(args):
            "sweep": []}
     for rate in rates:
         row = {"rate_per_s": rate}
-        for name, slots in (("served", args.slots), ("plain_per_request", 1)):
-            lat, wall, st = _serve_once(reqs, unit_gaps, slots, rate, args.budget_gb)
-            row[name] = _latency_row(lat, ns, alone, wall, terms, n_req, st, slots)
+        lat, wall, st = _serve_once(reqs, unit_gaps, args.slots, rate, args.budget_gb)
+        row["served"] = _latency_row(lat, ns, alone, wall, terms, n_req, st, args.slots)
+        lat, wall = _plain_once(reqs, unit_gaps, rate)
+        row["plain_per_request"] = _latency_row(lat, ns, alone, wall, terms, n_req, None, 1)
         out["sweep"].append(row)
+    # a burst of small expectation requests (n <= 14): what merging them into
+    # shared launch sequences buys over one call each
+    small = [r for r in reqs if r["kind"] == _abi.FPG_REQ_EXPECT and r["n"] <= 14]
+    if small:
+        burst = [dict(small[i % len(small)]) for i in range(args.burst)]
+        for r in burst:
+            r["out"] = torch.empty_like(r["out"])  # one output per request in flight
+        gaps = np.full(len(burst), 1.0)
+        bterms = sum(r["P"] * (1 << r["n"]) * r["S"] for r in burst)
+        bns = np.array([r["n"] for r in burst])
+        balone = np.zeros(len(burst))
+        lat, wall, st = _serve_once(burst, gaps, args.slots, args.burst_rate, args.budget_gb)
+        row = {"rate_per_s": args.burst_rate, "requests": len(burst),
+               "served": _latency_row(lat, bns, balone, wall, bterms, len(burst), st, args.slots)}
+        lat, wall = _plain_once(burst, gaps, args.burst_rate)
+        row["plain_per_request"] = _latency_row(lat, bns, balone, wall, bterms, len(burst), None, 1)
+        out["small_expectation_burst"] = row
     return out
 
 
@@ -1034,6 +1106,8 @@ def main():
     ap.add_argument("--max-n", type=int, default=24, help="serve: largest qubit count")
     ap.add_argument("--slots", type=int, default=8, help="serve: concurrent request slots")
     ap.add_argument("--budget-gb", type=int, default=64, help="serve: HBM budget for request scratch")
+    ap.add_argument("--burst", type=int, default=400, help="serve: small expectation requests in the burst")
+    ap.add_argument("--burst-rate", type=float, default=20000.0, help="serve: arrival rate of the burst (1/s)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

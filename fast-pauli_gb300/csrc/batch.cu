@@ -311,39 +311,58 @@ int max_resident(bool fp32, int bucket, int threads)
     return V == 1 ? max_resident_v<float, 1>(cls, threads) : max_resident_v<float, 2>(cls, threads);
 }
 
-int do_plan(fpg_batch *b, const fpg_batch_tuning &t)
+// Host side of a plan: per-problem entries (tiling, row splits, offsets of
+// the flattened reduction and contraction index spaces) and the work items
+// bucketed by (chunk class, V), largest problems first.  Device pointers of
+// the entries' partial tables are filled in by the caller (partial_off[i] =
+// the offset of problem i's table in one buffer of partial_total doubles).
+struct HostPlan
 {
-    if (t.threads_per_cta != 128 && t.threads_per_cta != 256)
-        return set_error(FPG_ERR_INVALID, "threads_per_cta must be 128 or 256");
-    if (t.ctas_per_sm < -1 || t.ctas_per_sm > 8)
-        return set_error(FPG_ERR_INVALID,
-                         "ctas_per_sm must be in [-1, 8] (0: as many as fit; -1: one CTA per work item)");
-    if (t.rows_per_item < 32 || (t.rows_per_item & (t.rows_per_item - 1)))
-        return set_error(FPG_ERR_INVALID, "rows_per_item must be a power of two >= 32");
-    if (t.tile_mb < 1)
-        return set_error(FPG_ERR_INVALID, "tile_mb must be >= 1");
-    b->free_plan();
-    const bool fp32 = b->dtype == FPG_C64;
-    const int np = (int)b->problems.size();
+    std::vector<BatchEntry> entries;
+    std::vector<BatchItem> items;
+    std::vector<int64_t> partial_off;
+    int bucket_begin[kBuckets + 1] = {};
+    int64_t red_total = 0, con_total = 0, partial_total = 0;
+};
+
+// Tiling of one problem, the rules of a single call: vector width,
+// L2-line-wide column tiles, and row windows (splits) only when a column tile
+// cannot stay in L2.
+void entry_tiling(const fpg_operator *op, int64_t S, const void *psi, bool fp32, const fpg_batch_tuning &t,
+                  int32_t &V, int32_t &TC, int32_t &n_splits)
+{
+    const int64_t tile_budget = (int64_t)t.tile_mb << 20;
+    V = (fp32 && S % 2 == 0 && ((uintptr_t)psi % 16) == 0) ? 2 : 1;
+    const int bpl = V * (fp32 ? 8 : 16);
+    TC = column_lanes_for_l2(std::min(tc_for((S + V - 1) / V), t.threads_per_cta), op->n, bpl, tile_budget);
+    const int64_t NB = op->n >= 5 ? ((int64_t)1 << (op->n - 5)) : 1;
+    const int64_t window = std::max<int64_t>(1, t.rows_per_item / 32);
+    n_splits = 1;
+    if (column_tile_footprint(TC, op->n, bpl) > tile_budget)
+        n_splits = (int32_t)std::max<int64_t>(1, std::min<int64_t>(256, (NB / 2 + window - 1) / window));
+}
+
+int plan_host(const std::vector<fpg_batch::Problem> &problems, bool fp32, const fpg_batch_tuning &t, HostPlan &hp)
+{
+    const int np = (int)problems.size();
     // largest problems first
     std::vector<int> order((size_t)np);
     for (int i = 0; i < np; ++i)
         order[(size_t)i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
-        const auto &pa = b->problems[(size_t)a], &pc = b->problems[(size_t)c];
+        const auto &pa = problems[(size_t)a], &pc = problems[(size_t)c];
         const double wa = (double)pa.op->P * (double)(1ll << pa.op->n) * (double)pa.S;
         const double wc = (double)pc.op->P * (double)(1ll << pc.op->n) * (double)pc.S;
         return wa > wc;
     });
-    std::vector<BatchEntry> entries((size_t)np);
+    hp.entries.assign((size_t)np, BatchEntry{});
     std::vector<std::vector<BatchItem>> by_bucket(kBuckets);
-    const int64_t tile_budget = (int64_t)t.tile_mb << 20;
     for (int pos = 0; pos < np; ++pos)
     {
         const int i = order[(size_t)pos];
-        const auto &p = b->problems[(size_t)i];
+        const auto &p = problems[(size_t)i];
         const fpg_operator *op = p.op;
-        BatchEntry &e = entries[(size_t)i];
+        BatchEntry &e = hp.entries[(size_t)i];
         e.psi = p.psi;
         e.recs = op->d_recs;
         e.orig = op->d_orig;
@@ -354,17 +373,7 @@ int do_plan(fpg_batch *b, const fpg_batch_tuning &t)
         e.P = op->P;
         e.K = p.K;
         e.n = op->n;
-        // same tiling rules as a single call: vector width, L2-line-wide column
-        // tiles, and row windows (splits) only when a tile cannot stay in L2
-        e.V = (fp32 && p.S % 2 == 0 && ((uintptr_t)p.psi % 16) == 0) ? 2 : 1;
-        const int bpl = e.V * (fp32 ? 8 : 16);
-        e.TC = column_lanes_for_l2(std::min(tc_for((p.S + e.V - 1) / e.V), t.threads_per_cta), op->n, bpl,
-                                   tile_budget);
-        const int64_t NB = op->n >= 5 ? ((int64_t)1 << (op->n - 5)) : 1;
-        const int64_t window = std::max<int64_t>(1, t.rows_per_item / 32);
-        e.n_splits = 1;
-        if (column_tile_footprint(e.TC, op->n, bpl) > tile_budget)
-            e.n_splits = (int32_t)std::max<int64_t>(1, std::min<int64_t>(256, (NB / 2 + window - 1) / window));
+        entry_tiling(op, p.S, p.psi, fp32, t, e.V, e.TC, e.n_splits);
         const int64_t ctiles = (e.S + (int64_t)e.TC * e.V - 1) / ((int64_t)e.TC * e.V);
         for (int c = 0; c < kNumChunkClasses; ++c)
         {
@@ -375,41 +384,71 @@ int do_plan(fpg_batch *b, const fpg_batch_tuning &t)
                         dst.push_back(BatchItem{i, ch, (int32_t)ct, s});
         }
     }
-    std::vector<BatchItem> items;
+    hp.items.clear();
     for (int k = 0; k < kBuckets; ++k)
     {
-        b->bucket_begin[k] = (int)items.size();
-        items.insert(items.end(), by_bucket[(size_t)k].begin(), by_bucket[(size_t)k].end());
+        hp.bucket_begin[k] = (int)hp.items.size();
+        hp.items.insert(hp.items.end(), by_bucket[(size_t)k].begin(), by_bucket[(size_t)k].end());
     }
-    b->bucket_begin[kBuckets] = (int)items.size();
-    if (items.size() > (size_t)0x7fffffff)
+    hp.bucket_begin[kBuckets] = (int)hp.items.size();
+    if (hp.items.size() > (size_t)0x7fffffff)
         return set_error(FPG_ERR_UNSUPPORTED, "batch has too many work items");
     // entries keep the order of addition: partial tables and the flattened
     // index spaces of reduction and contraction are laid out in that order
-    int64_t partial_total = 0, red_off = 0, con_off = 0;
+    hp.partial_off.assign((size_t)np, 0);
+    int64_t red_off = 0, con_off = 0, partial_total = 0;
     for (int i = 0; i < np; ++i)
     {
-        BatchEntry &e = entries[(size_t)i];
+        BatchEntry &e = hp.entries[(size_t)i];
         e.red_off = red_off;
         e.con_off = con_off;
         red_off += e.P * e.S;
         con_off += e.K * e.S;
+        hp.partial_off[(size_t)i] = partial_total;
         partial_total += (int64_t)e.n_splits * e.P * e.S;
     }
-    b->red_total = red_off;
-    b->con_total = con_off;
+    hp.red_total = red_off;
+    hp.con_total = con_off;
+    hp.partial_total = partial_total;
+    return FPG_OK;
+}
+
+int check_tuning(const fpg_batch_tuning &t)
+{
+    if (t.threads_per_cta != 128 && t.threads_per_cta != 256)
+        return set_error(FPG_ERR_INVALID, "threads_per_cta must be 128 or 256");
+    if (t.ctas_per_sm < -1 || t.ctas_per_sm > 8)
+        return set_error(FPG_ERR_INVALID,
+                         "ctas_per_sm must be in [-1, 8] (0: as many as fit; -1: one CTA per work item)");
+    if (t.rows_per_item < 32 || (t.rows_per_item & (t.rows_per_item - 1)))
+        return set_error(FPG_ERR_INVALID, "rows_per_item must be a power of two >= 32");
+    if (t.tile_mb < 1)
+        return set_error(FPG_ERR_INVALID, "tile_mb must be >= 1");
+    return FPG_OK;
+}
+
+int do_plan(fpg_batch *b, const fpg_batch_tuning &t)
+{
+    if (int rc = check_tuning(t))
+        return rc;
+    b->free_plan();
+    const bool fp32 = b->dtype == FPG_C64;
+    HostPlan hp;
+    if (int rc = plan_host(b->problems, fp32, t, hp))
+        return rc;
+    std::copy(hp.bucket_begin, hp.bucket_begin + kBuckets + 1, b->bucket_begin);
+    b->red_total = hp.red_total;
+    b->con_total = hp.con_total;
     cudaError_t err = cudaSuccess;
-    if ((err = cudaMalloc((void **)&b->d_partial, (size_t)std::max<int64_t>(1, partial_total) * sizeof(double))))
+    if ((err = cudaMalloc((void **)&b->d_partial, (size_t)std::max<int64_t>(1, hp.partial_total) * sizeof(double))))
     {
         b->free_plan();
         return cuda_error(err, "fpg_batch_plan: partial tables");
     }
-    int64_t off = 0;
-    for (int i = 0; i < np; ++i)
-    {
-        entries[(size_t)i].partial = b->d_partial + off;
-        off += (int64_t)entries[(size_t)i].n_splits * entries[(size_t)i].P * entries[(size_t)i].S;
-    }
+    for (size_t i = 0; i < hp.entries.size(); ++i)
+        hp.entries[i].partial = b->d_partial + hp.partial_off[i];
+    auto &entries = hp.entries;
+    auto &items = hp.items;
     if ((err = cudaMalloc((void **)&b->d_entries, entries.size() * sizeof(BatchEntry))) ||
         (err = cudaMemcpy(b->d_entries, entries.data(), entries.size() * sizeof(BatchEntry),
                           cudaMemcpyHostToDevice)) ||
@@ -429,45 +468,115 @@ int do_plan(fpg_batch *b, const fpg_batch_tuning &t)
     return FPG_OK;
 }
 
-int do_run(fpg_batch *b, cudaStream_t st)
+// The launch sequence of a run: counter reset, one kernel per non-empty
+// bucket, the split reduction and the contraction (outputs overwritten).
+int launch_sequence(bool fp32, const fpg_batch_tuning &t, int grid_cap, const BatchEntry *d_entries,
+                    const BatchItem *d_items, int *d_counters, const int *bucket_begin, int np, int64_t red_total,
+                    int64_t con_total, cudaStream_t st)
 {
-    const bool fp32 = b->dtype == FPG_C64;
     cudaError_t e;
-    if ((e = cudaMemsetAsync(b->d_counters, 0, kBuckets * sizeof(int), st)))
+    if ((e = cudaMemsetAsync(d_counters, 0, kBuckets * sizeof(int), st)))
         return cuda_error(e, "cudaMemsetAsync");
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+    const int sms = sm_count();
     for (int k = 0; k < kBuckets; ++k)
     {
-        const int n_items = b->bucket_begin[k + 1] - b->bucket_begin[k];
+        const int n_items = bucket_begin[k + 1] - bucket_begin[k];
         if (n_items <= 0)
             continue;
         int grid = -1; // item-grid form
-        if (b->tuning.ctas_per_sm >= 0)
+        if (t.ctas_per_sm >= 0)
         {
-            const int cap = sms * max_resident(fp32, k, b->tuning.threads_per_cta);
-            grid = std::max(1, std::min({b->grid, cap, n_items}));
+            const int cap = sms * max_resident(fp32, k, t.threads_per_cta);
+            grid = std::max(1, std::min({grid_cap, cap, n_items}));
         }
-        if ((e = launch_bucket(fp32, k, grid, b->tuning.threads_per_cta, b->d_entries, b->d_items + b->bucket_begin[k],
-                               n_items, b->d_counters + k, st)))
+        if ((e = launch_bucket(fp32, k, grid, t.threads_per_cta, d_entries, d_items + bucket_begin[k], n_items,
+                               d_counters + k, st)))
             return cuda_error(e, "persistent batch kernel");
     }
-    const int np = (int)b->problems.size();
-    const unsigned g1 = (unsigned)std::max<int64_t>(1, std::min<int64_t>((b->red_total + 255) / 256, sms * 16));
-    k_batch_reduce<<<g1, 256, 0, st>>>(b->d_entries, np, b->red_total);
+    const unsigned g1 = (unsigned)std::max<int64_t>(1, std::min<int64_t>((red_total + 255) / 256, sms * 16));
+    k_batch_reduce<<<g1, 256, 0, st>>>(d_entries, np, red_total);
     if ((e = launched()))
         return cuda_error(e, "batch reduction");
-    const unsigned g2 = (unsigned)std::max<int64_t>(1, std::min<int64_t>((b->con_total + 255) / 256, sms * 16));
+    const unsigned g2 = (unsigned)std::max<int64_t>(1, std::min<int64_t>((con_total + 255) / 256, sms * 16));
     if (fp32)
-        k_batch_contract<float2><<<g2, 256, 0, st>>>(b->d_entries, np, b->con_total);
+        k_batch_contract<float2><<<g2, 256, 0, st>>>(d_entries, np, con_total);
     else
-        k_batch_contract<double2><<<g2, 256, 0, st>>>(b->d_entries, np, b->con_total);
+        k_batch_contract<double2><<<g2, 256, 0, st>>>(d_entries, np, con_total);
     if ((e = launched()))
         return cuda_error(e, "batch contraction");
     return FPG_OK;
 }
 
+int do_run(fpg_batch *b, cudaStream_t st)
+{
+    return launch_sequence(b->dtype == FPG_C64, b->tuning, b->grid, b->d_entries, b->d_items, b->d_counters,
+                           b->bucket_begin, (int)b->problems.size(), b->red_total, b->con_total, st);
+}
+
 } // namespace
+
+namespace fpg
+{
+// Expectation problems run as one batch, stream-ordered: the work queue and
+// the partial tables come from the library's pool on `st` and go back to it
+// on `st` after the run, and the host arrays are uploaded with asynchronous
+// copies, so nothing synchronises the device (the serving loop merges the
+// small expectation requests it admits together this way).  Default tuning;
+// outputs are overwritten.  A problem's result does not depend on the other
+// problems of the run (every summation order is fixed per problem).
+int run_merged_expect(int32_t dtype, const MergedExpect *probs, int n, cudaStream_t st)
+{
+    if (n <= 0)
+        return FPG_OK;
+    std::vector<fpg_batch::Problem> problems((size_t)n);
+    for (int i = 0; i < n; ++i)
+        problems[(size_t)i] = fpg_batch::Problem{probs[i].op, probs[i].coeffs, probs[i].n_operators,
+                                                  probs[i].states, probs[i].out, probs[i].n_states};
+    const bool fp32 = dtype == FPG_C64;
+    const fpg_batch_tuning t{256, 0, 1 << 15, 40};
+    HostPlan hp;
+    if (int rc = plan_host(problems, fp32, t, hp))
+        return rc;
+    const size_t b_partial = (size_t)std::max<int64_t>(1, hp.partial_total) * sizeof(double);
+    const size_t b_entries = hp.entries.size() * sizeof(BatchEntry);
+    const size_t b_items = std::max<size_t>(1, hp.items.size()) * sizeof(BatchItem);
+    const size_t b_counters = kBuckets * sizeof(int);
+    auto al = [](size_t v) { return (v + 255) & ~size_t(255); };
+    void *buf = nullptr;
+    if (int rc = fpg_device_alloc(&buf, al(b_partial) + al(b_entries) + al(b_items) + b_counters, st))
+        return rc;
+    char *base = (char *)buf;
+    double *d_partial = (double *)base;
+    BatchEntry *d_entries = (BatchEntry *)(base + al(b_partial));
+    BatchItem *d_items = (BatchItem *)(base + al(b_partial) + al(b_entries));
+    int *d_counters = (int *)(base + al(b_partial) + al(b_entries) + al(b_items));
+    for (size_t i = 0; i < hp.entries.size(); ++i)
+        hp.entries[i].partial = d_partial + hp.partial_off[i];
+    cudaError_t e;
+    int rc = FPG_OK;
+    // pageable sources: each copy has read its source when it returns
+    if ((e = cudaMemcpyAsync(d_entries, hp.entries.data(), b_entries, cudaMemcpyHostToDevice, st)) ||
+        (!hp.items.empty() &&
+         (e = cudaMemcpyAsync(d_items, hp.items.data(), hp.items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice,
+                              st))))
+        rc = cuda_error(e, "cudaMemcpyAsync (merged batch plan)");
+    if (rc == FPG_OK)
+        rc = launch_sequence(fp32, t, 1 << 30, d_entries, d_items, d_counters, hp.bucket_begin, n, hp.red_total,
+                             hp.con_total, st);
+    fpg_device_free(buf, st);
+    return rc;
+}
+
+size_t merged_expect_scratch_bytes(const fpg_operator *op, int64_t S, const void *states, bool fp32)
+{
+    int32_t V = 1, TC = 1, n_splits = 1;
+    entry_tiling(op, S, states, fp32, fpg_batch_tuning{256, 0, 1 << 15, 40}, V, TC, n_splits);
+    const int64_t ctiles = (S + (int64_t)TC * V - 1) / ((int64_t)TC * V);
+    const int64_t items = (int64_t)op->chunks.size() * ctiles * n_splits;
+    return (size_t)(n_splits * op->P * S) * sizeof(double) + (size_t)items * sizeof(BatchItem) + sizeof(BatchEntry) +
+           4 * 256 + kBuckets * sizeof(int);
+}
+} // namespace fpg
 
 extern "C"
 {

@@ -136,10 +136,12 @@ __device__ __forceinline__ void expect_chunk_body(const T *__restrict__ psi, int
             const T *pa0 = psi + 2 * ((int64_t)base * S + t0);
             // rows in groups of RG: all loads of a group are issued before any
             // is consumed.  Single-string float32 chunks (random strings) have
-            // almost no arithmetic per row and batch 4 rows of loads; every
-            // other class keeps its registers for occupancy (measured: deeper
-            // batches cost the weight-2 float32 classes a CTA per SM).
-            constexpr int RG = (sizeof(T) == 4 && G == 1) ? 4 : 1;
+            // almost no arithmetic per row and are bound by load latency: they
+            // batch as many rows as fit the three-CTA register budget without
+            // spilling (8 rows of one-column lanes, 5 of two-column lanes);
+            // every other class keeps its registers for occupancy (measured:
+            // deeper batches cost the weight-2 float32 classes a CTA per SM).
+            constexpr int RG = (sizeof(T) == 4 && G == 1) ? (V == 1 ? 8 : 5) : 1;
 #pragma unroll
             for (int r0 = 0; r0 < 32; r0 += RG)
             {

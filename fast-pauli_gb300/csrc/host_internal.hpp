@@ -30,6 +30,23 @@ namespace fpg
 // Upper bound of the scratch bytes one expectation (weighted = false) or
 // apply_weighted (weighted = true) call draws from the stream-ordered pool.
 size_t request_scratch_bytes(const fpg_operator *op, int64_t K, int64_t S, bool fp32, bool weighted);
+
+// One expectation problem of a merged run: out(K,S) = sum_j coeffs(j,k)
+// <psi_t|P_j|psi_t> (overwritten), device arrays of the run's dtype.
+struct MergedExpect
+{
+    const fpg_operator *op;
+    const void *coeffs;
+    int64_t n_operators;
+    const void *states;
+    void *out;
+    int64_t n_states;
+};
+// Problems run as one batch on `st` without synchronising (batch.cu); each
+// problem's result is independent of the others in the run.
+int run_merged_expect(int32_t dtype, const MergedExpect *probs, int n, cudaStream_t st);
+// Pool bytes one problem adds to a merged run (upper bound for admission).
+size_t merged_expect_scratch_bytes(const fpg_operator *op, int64_t S, const void *states, bool fp32);
 } // namespace fpg
 
 // An encoded operator: host copies of the encoding and their device mirrors.

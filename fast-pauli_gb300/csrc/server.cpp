@@ -25,8 +25,17 @@
 //    and memory free up, while earlier requests are still running; admitted
 //    requests run concurrently on their slots' streams, so their kernels
 //    overlap on the device.
-//  * Each request runs the same deterministic kernels it would run alone, so
-//    its result does not depend on the mix (tests check this).
+//  * Batching: small expectation requests (the small class above) always run
+//    through the merged path (run_merged_expect, batch.cu): every such
+//    request admitted in one scheduling round -- those that arrived while
+//    the GPU was busy, up to kMaxMerge -- shares one launch sequence (one
+//    work-queue kernel per chunk class, one reduction, one contraction) on
+//    one slot, instead of a stream and ~10 launches each.  A request alone
+//    runs the same path as a merge of one.
+//  * Each request runs the same deterministic kernels it would run alone
+//    (the merged path's per-request results do not depend on the other
+//    requests of the merge), so its result does not depend on the mix
+//    (tests check this).
 //  * Outputs are overwritten (zeroed, then computed).
 //  * Latency per ticket: submit -> admission -> completion (host steady
 //    clock, completion observed through a CUDA event).
@@ -66,8 +75,12 @@ struct Ticket
     std::string err;
     clock_type::time_point t_submit, t_start, t_done;
     int slot = -1;
-    int tier = 2; // 0 small, 1 medium, 2 large
+    int tier = 2;       // 0 small, 1 medium, 2 large
+    bool merge = false; // small expectation request: the merged path
 };
+
+// Most small expectation requests one merged launch sequence takes.
+constexpr int kMaxMerge = 64;
 
 // Work classes in amplitude-terms (n_strings * 2^n * n_states): small is a
 // few milliseconds of GPU time, medium up to ~0.2 s.
@@ -94,7 +107,7 @@ struct fpg_server
     {
         cudaStream_t stream = nullptr;
         cudaEvent_t event = nullptr;
-        uint64_t ticket = 0;
+        std::vector<uint64_t> tickets; // one request, or the requests of a merged run
         bool busy = false;
         int tier = 2; // 0: the device's highest stream priority, 1: middle, 2: lowest
     };
@@ -105,12 +118,41 @@ struct fpg_server
     std::thread worker;
     // counters
     uint64_t completed = 0, failed = 0, refused = 0;
+    uint64_t merged_runs = 0, merged_requests = 0;
     size_t peak_reserved = 0;
     int peak_running = 0;
 
     void run();
     int dispatch(Slot &s, Ticket &t);
+    int dispatch_merged(Slot &s, const std::vector<uint64_t> &ids);
+    std::vector<Slot>::iterator free_slot_for(int tier);
 };
+
+std::vector<fpg_server::Slot>::iterator fpg_server::free_slot_for(int tier)
+{
+    // a free slot of the request's tier, else of a lower-priority tier:
+    // higher tiers stay free for the shorter requests
+    auto it = slots.end();
+    for (int tr = tier; tr <= 2 && it == slots.end(); ++tr)
+        it = std::find_if(slots.begin(), slots.end(), [tr](const Slot &s) { return !s.busy && s.tier == tr; });
+    return it;
+}
+
+int fpg_server::dispatch_merged(Slot &s, const std::vector<uint64_t> &ids)
+{
+    std::vector<MergedExpect> probs;
+    probs.reserve(ids.size());
+    for (uint64_t id : ids)
+    {
+        const fpg_request &r = tickets[id].req;
+        probs.push_back(MergedExpect{r.op, r.coeffs, r.n_operators, r.states, r.out, r.n_states});
+    }
+    if (int rc = run_merged_expect(cfg.dtype, probs.data(), (int)probs.size(), s.stream))
+        return rc;
+    if (cudaError_t e = cudaEventRecord(s.event, s.stream))
+        return cuda_error(e, "cudaEventRecord");
+    return FPG_OK;
+}
 
 int fpg_server::dispatch(Slot &s, Ticket &t)
 {
@@ -159,44 +201,68 @@ void fpg_server::run()
                 ++running;
                 continue;
             }
-            Ticket &t = tickets[s.ticket];
-            t.t_done = clock_type::now();
-            if (q == cudaSuccess)
+            const auto now = clock_type::now();
+            for (uint64_t id : s.tickets)
             {
-                t.status = 2;
-                ++completed;
+                Ticket &t = tickets[id];
+                t.t_done = now;
+                if (q == cudaSuccess)
+                {
+                    t.status = 2;
+                    ++completed;
+                }
+                else
+                {
+                    t.status = 3;
+                    t.rc = FPG_ERR_CUDA;
+                    t.err = cudaGetErrorString(q);
+                    ++failed;
+                }
+                reserved -= t.need;
             }
-            else
-            {
-                t.status = 3;
-                t.rc = FPG_ERR_CUDA;
-                t.err = cudaGetErrorString(q);
-                ++failed;
-            }
-            reserved -= t.need;
+            s.tickets.clear();
             s.busy = false;
             progressed = true;
         }
         if (progressed)
             cv_done.notify_all();
-        // 2. admit queued requests into free slots while the budget allows
+        // 2. admit queued requests into free slots while the budget allows;
+        // small expectation requests admitted in this round go to one merged
+        // run on one slot
+        auto merge_slot = slots.end();
+        std::vector<uint64_t> merge_ids;
         for (auto it = queue.begin(); it != queue.end();)
         {
             Ticket &t = tickets[*it];
-            // a free slot of the request's tier, else of a lower-priority tier:
-            // higher tiers stay free for the shorter requests
-            auto free_slot = slots.end();
-            for (int tier = t.tier; tier <= 2 && free_slot == slots.end(); ++tier)
-                free_slot = std::find_if(slots.begin(), slots.end(),
-                                         [tier](const Slot &s) { return !s.busy && s.tier == tier; });
-            if (free_slot == slots.end())
-            {
-                ++it; // no slot of its class: later requests of the other class may pass
-                continue;
-            }
             if (reserved + t.need > (size_t)cfg.hbm_budget_bytes)
             {
                 ++it; // does not fit yet: let later, smaller requests pass
+                continue;
+            }
+            if (t.merge)
+            {
+                if (merge_slot == slots.end())
+                    merge_slot = free_slot_for(t.tier);
+                if (merge_slot == slots.end() || (int)merge_ids.size() >= kMaxMerge)
+                {
+                    ++it;
+                    continue;
+                }
+                merge_slot->busy = true; // held for the merged run dispatched below
+                reserved += t.need;
+                peak_reserved = std::max(peak_reserved, reserved);
+                t.status = 1;
+                t.t_start = clock_type::now();
+                t.slot = (int)(merge_slot - slots.begin());
+                merge_ids.push_back(*it);
+                it = queue.erase(it);
+                progressed = true;
+                continue;
+            }
+            auto free_slot = free_slot_for(t.tier);
+            if (free_slot == slots.end())
+            {
+                ++it; // no slot of its class: later requests of the other class may pass
                 continue;
             }
             reserved += t.need;
@@ -218,11 +284,38 @@ void fpg_server::run()
             else
             {
                 free_slot->busy = true;
-                free_slot->ticket = *it;
+                free_slot->tickets.assign(1, *it);
                 ++running;
             }
             it = queue.erase(it);
             progressed = true;
+        }
+        if (!merge_ids.empty())
+        {
+            const int rc = dispatch_merged(*merge_slot, merge_ids);
+            if (rc != FPG_OK)
+            {
+                const std::string err = fpg_last_error();
+                for (uint64_t id : merge_ids)
+                {
+                    Ticket &t = tickets[id];
+                    t.status = 3;
+                    t.rc = rc;
+                    t.err = err;
+                    t.t_done = clock_type::now();
+                    reserved -= t.need;
+                    ++failed;
+                }
+                merge_slot->busy = false;
+                cv_done.notify_all();
+            }
+            else
+            {
+                merge_slot->tickets = merge_ids;
+                ++merged_runs;
+                merged_requests += merge_ids.size();
+                ++running;
+            }
         }
         peak_running = std::max(peak_running, running);
         if (stop && queue.empty() && running == 0)
@@ -309,8 +402,15 @@ extern "C"
             return set_error(FPG_ERR_INVALID, "null array in request");
         if (req->n_operators < 1 || req->n_states < 1)
             return set_error(FPG_ERR_INVALID, "n_operators and n_states must be >= 1");
-        const size_t need = request_scratch_bytes(req->op, req->n_operators, req->n_states,
-                                                  s->cfg.dtype == FPG_C64, req->kind == FPG_REQ_APPLY_WEIGHTED);
+        int32_t nq = 0;
+        int64_t ps = 0;
+        fpg_operator_info(req->op, &nq, &ps, nullptr);
+        const int tier = work_tier((double)ps * std::ldexp(1.0, nq) * (double)req->n_states);
+        const bool merge = req->kind == FPG_REQ_EXPECT && tier == 0;
+        const size_t need =
+            merge ? merged_expect_scratch_bytes(req->op, req->n_states, req->states, s->cfg.dtype == FPG_C64)
+                  : request_scratch_bytes(req->op, req->n_operators, req->n_states, s->cfg.dtype == FPG_C64,
+                                          req->kind == FPG_REQ_APPLY_WEIGHTED);
         std::lock_guard<std::mutex> lk(s->mu);
         if (s->stop)
             return set_error(FPG_ERR_INVALID, "server is shutting down");
@@ -329,12 +429,8 @@ extern "C"
         Ticket t;
         t.req = *req;
         t.need = need;
-        {
-            int32_t nq = 0;
-            int64_t ps = 0;
-            fpg_operator_info(req->op, &nq, &ps, nullptr);
-            t.tier = work_tier((double)ps * std::ldexp(1.0, nq) * (double)req->n_states);
-        }
+        t.tier = tier;
+        t.merge = merge;
         t.t_submit = clock_type::now();
         s->tickets.emplace(id, std::move(t));
         s->queue.push_back(id);
@@ -399,6 +495,8 @@ extern "C"
         st->queued = (int64_t)s->queue.size();
         st->peak_running = s->peak_running;
         st->peak_reserved_bytes = (int64_t)s->peak_reserved;
+        st->merged_runs = (int64_t)s->merged_runs;
+        st->merged_requests = (int64_t)s->merged_requests;
         return FPG_OK;
     }
 

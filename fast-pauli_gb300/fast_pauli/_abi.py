@@ -93,7 +93,8 @@ class TicketInfo(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [("completed", ctypes.c_int64), ("failed", ctypes.c_int64), ("refused", ctypes.c_int64),
                 ("queued", ctypes.c_int64), ("peak_running", ctypes.c_int32), ("reserved", ctypes.c_int32),
-                ("peak_reserved_bytes", ctypes.c_int64)]
+                ("peak_reserved_bytes", ctypes.c_int64), ("merged_runs", ctypes.c_int64),
+                ("merged_requests", ctypes.c_int64)]
 
 
 SIGNATURES.update({
@@ -230,7 +231,8 @@ class Server:
         s = ServerStats()
         check(lib().fpg_server_stats(self._h, ctypes.byref(s)))
         return {"completed": s.completed, "failed": s.failed, "refused": s.refused, "queued": s.queued,
-                "peak_running": s.peak_running, "peak_reserved_bytes": s.peak_reserved_bytes}
+                "peak_running": s.peak_running, "peak_reserved_bytes": s.peak_reserved_bytes,
+                "merged_runs": s.merged_runs, "merged_requests": s.merged_requests}
 
     def close(self) -> None:
         if self._h:

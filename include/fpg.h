@@ -266,7 +266,12 @@ int fpg_batch_destroy(fpg_batch *batch);
  * budget, so requests arriving while others run are started immediately and
  * overlap on the device.  A request needing more than the whole budget, or
  * arriving at a full queue, is refused with FPG_ERR_BUSY.  Outputs are
- * overwritten.  Results do not depend on the mix (same kernels as alone).
+ * overwritten.  Small expectation requests (n_strings x 2^n x n_states <= 4e9)
+ * admitted in the same scheduling round run as one merged batch (one
+ * work-queue kernel per chunk class, one reduction, one contraction) on one
+ * slot; alone, such a request runs as a merge of one.  Results do not depend
+ * on the mix (a request runs the same kernels, in the same summation order,
+ * alone and in the mix).
  * ------------------------------------------------------------------------ */
 enum fpg_request_kind
 {
@@ -309,6 +314,8 @@ typedef struct fpg_server_stats_t
     int32_t peak_running;
     int32_t reserved;
     int64_t peak_reserved_bytes;
+    int64_t merged_runs;     /* merged launch sequences of small expectation requests */
+    int64_t merged_requests; /* requests those runs served                            */
 } fpg_server_stats_t;
 
 typedef struct fpg_server fpg_server;

@@ -77,6 +77,9 @@ def test_results_same_alone_and_in_the_mix(dtype_name):
     srv.close()
     assert stats["completed"] == len(reqs) and stats["failed"] == 0
     assert stats["peak_running"] >= 2  # requests overlapped on the device
+    # every expectation request here is small: all ran through merged runs
+    n_expect = sum(r["kind"] == _abi.FPG_REQ_EXPECT for r in reqs)
+    assert stats["merged_requests"] == n_expect and 1 <= stats["merged_runs"] <= n_expect
     for r, (t, out), a, info in zip(reqs, pending, alone, infos):
         got = out.cpu().numpy()
         np.testing.assert_array_equal(got, a)  # identical alone and in the mix
@@ -86,6 +89,48 @@ def test_results_same_alone_and_in_the_mix(dtype_name):
             want = oracle.summed_apply_weighted(r["strings"], r["h"], r["psi"], r["data"])
         assert normwise(got, want) < tol
         assert info["submit_us"] <= info["start_us"] <= info["done_us"]
+
+
+def test_small_requests_queued_together_share_one_merged_run():
+    """Small expectation requests that queue while the only slot is busy are
+    admitted together into one merged run (one launch sequence for all of
+    them); each result is bit-identical to the request served alone and
+    matches the oracle."""
+    torch = pytest.importorskip("torch")
+    from fast_pauli import _abi
+
+    rng = np.random.default_rng(17)
+    cdt = torch.complex128
+    small = [r for r in _make_requests(torch, rng, 24, cdt, torch.float64) if r["kind"] == _abi.FPG_REQ_EXPECT]
+    # a medium request that keeps the slot busy while the small ones arrive
+    n, P, S = 18, 1000, 32
+    strings = oracle.uniform_strings(rng, n, P)
+    big = dict(kind=_abi.FPG_REQ_EXPECT, op=_abi.Operator(strings), K=1, S=S, out_shape=(1, S),
+               dev={"h": torch.ones((P, 1), dtype=cdt, device="cuda"),
+                    "psi": torch.randn((1 << n, S), dtype=cdt, device="cuda"),
+                    "data": torch.zeros(1, device="cuda")})
+    alone = []
+    srv = _abi.Server(_abi.FPG_C128, n_slots=1)
+    for r in small:
+        t, out = _submit(srv, torch, r, cdt)
+        srv.wait(t)
+        alone.append(out.cpu().numpy())
+    srv.close()
+
+    srv = _abi.Server(_abi.FPG_C128, n_slots=1)
+    tb, _ = _submit(srv, torch, big, cdt)
+    pending = [_submit(srv, torch, r, cdt) for r in small]
+    srv.wait(tb, timeout_ms=60000)
+    for t, _ in pending:
+        srv.wait(t, timeout_ms=60000)
+    st = srv.stats()
+    srv.close()
+    assert st["failed"] == 0 and st["merged_requests"] == len(small)
+    assert st["merged_runs"] < len(small)  # at least two requests shared a run
+    for r, (t, out), a in zip(small, pending, alone):
+        got = out.cpu().numpy()
+        np.testing.assert_array_equal(got, a)
+        assert normwise(got, oracle.summed_expectation(r["strings"], r["h"], r["psi"])) < TOL_C128
 
 
 def test_admission_by_hbm_budget_and_refusals():
