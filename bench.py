@@ -1060,6 +1060,8 @@ def serve_summary(n_req=40, rate=4.0, max_n=24, slots=8, budget_gb=64):
     import numpy as np
     import torch
 
+    from fast_pauli import _abi
+
     reqs, unit_gaps = _serve_requests(n_req, max_n)
     terms = sum(r["P"] * (1 << r["n"]) * r["S"] for r in reqs)
     ns = np.array([r["n"] for r in reqs])
@@ -1068,6 +1070,25 @@ def serve_summary(n_req=40, rate=4.0, max_n=24, slots=8, budget_gb=64):
     lat, wall, st = _serve_once(reqs, unit_gaps, slots, rate, budget_gb)
     row = _latency_row(lat, ns, alone, wall, terms, n_req, st, slots)
     slow = (ns <= 20) & (alone >= 10.0)
+    # a burst of small expectation requests arriving faster than they are
+    # served: queued ones are merged into shared runs
+    burst = None
+    small = [r for r in reqs if r["kind"] == _abi.FPG_REQ_EXPECT and r["n"] <= 14]
+    if small:
+        breqs = [dict(small[i % len(small)]) for i in range(200)]
+        for r in breqs:
+            r["out"] = torch.empty_like(r["out"])
+        gaps = np.full(len(breqs), 1.0)
+        blat, bwall, bst = _serve_once(breqs, gaps, slots, 20000.0, budget_gb)
+        plat, pwall = _plain_once(breqs, gaps, 20000.0)
+        burst = {"requests": len(breqs), "rate_per_s": 20000.0,
+                 "served": {"p50_ms": float(np.percentile(blat, 50)), "p99_ms": float(np.percentile(blat, 99)),
+                            "requests_per_s": len(breqs) / bwall, "merged_runs": bst["merged_runs"],
+                            "merged_requests": bst["merged_requests"]},
+                 "plain_per_request": {"p50_ms": float(np.percentile(plat, 50)),
+                                       "p99_ms": float(np.percentile(plat, 99)),
+                                       "requests_per_s": len(breqs) / pwall}}
+        del breqs
     out = {"workload": f"{n_req} requests, Poisson {rate}/s, n~U{{10..{max_n}}}, P log-uniform 32..2048 uniform "
                        "strings, S~U{1..64}, K log-uniform 1..64, 50/50 expectation_value / apply_weighted, "
                        "complex64, 8 slots",
@@ -1075,7 +1096,8 @@ def serve_summary(n_req=40, rate=4.0, max_n=24, slots=8, budget_gb=64):
            "service_alone_ms": {"p50": float(np.percentile(alone, 50)), "p99": float(np.percentile(alone, 99))},
            "n_le_20_over_10ms_alone": {"count": int(slow.sum()),
                                        "min_terms": float(work[slow].min()) if slow.any() else None,
-                                       "min_alone_ms": float(alone[slow].min()) if slow.any() else None}}
+                                       "min_alone_ms": float(alone[slow].min()) if slow.any() else None},
+           "small_expectation_burst": burst}
     del reqs
     torch.cuda.empty_cache()
     return out
