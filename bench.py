@@ -428,7 +428,7 @@ def run_profile_batch(args):
     stream = _stream_handle()
     g = torch.Generator(device="cuda").manual_seed(4)
     items = []
-    for n, strings, c, S in _cfg4_problems():
+    for n, strings, c, S in _uneven_problems():
         D = 1 << n
         psi = torch.complex(torch.randn(D, S, device="cuda", generator=g),
                             torch.randn(D, S, device="cuda", generator=g))
@@ -568,7 +568,7 @@ def run_reference(args, rank, world):
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
-def _cfg4_problems(seed=1004, count=256):
+def _uneven_problems(seed=1004, count=256):
     """Uneven batch: n ~ U{8..20}, strings log-uniform in [16, 4096]
     (uniform random strings), states ~ U{1..256}."""
     import numpy as np
@@ -774,7 +774,7 @@ def run_batch(args):
 
     torch.cuda.set_device(0)
     L = _abi.lib()
-    probs = _cfg4_problems()
+    probs = _uneven_problems()
     stream = _stream_handle()
     g = torch.Generator(device="cuda").manual_seed(4)
     items = []
