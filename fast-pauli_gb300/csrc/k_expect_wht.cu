@@ -76,6 +76,10 @@ struct W32
     {
         return v;
     }
+    static __device__ __forceinline__ val from_cell(cell c)
+    {
+        return c;
+    }
     static __device__ __forceinline__ void add_cell(val &s, cell c, bool neg)
     {
         s += neg ? -c : c;
@@ -130,6 +134,10 @@ struct W64
     static __device__ __forceinline__ cell to_cell(val v)
     {
         return v;
+    }
+    static __device__ __forceinline__ val from_cell(cell c)
+    {
+        return c;
     }
     static __device__ __forceinline__ void add_cell(val &s, cell c, bool neg)
     {
@@ -193,6 +201,10 @@ struct WDF
     {
         df_norm(v.h, v.l);
         return make_float2(v.h, v.l);
+    }
+    static __device__ __forceinline__ val from_cell(cell c)
+    {
+        return DFv{c.x, c.y};
     }
     static __device__ __forceinline__ void add_cell(val &s, cell c, bool neg)
     {
@@ -267,6 +279,33 @@ __device__ __forceinline__ void rows_q(const typename W::in_t *__restrict__ psi,
     }
 }
 
+// Second level: in place over the round's TR2 blocks, for every (part,
+// coefficient u, column lane): W2[v] = sum_rr (-1)^popc(rr & v) W[rr].
+template <typename W, int TR2>
+__device__ __forceinline__ void wht_rounds(typename W::cell *wsm, int TR, int TC, int first_part, int parts)
+{
+    using val = typename W::val;
+    for (int idx = threadIdx.x; idx < parts * 16 * TC; idx += blockDim.x)
+    {
+        const int pi = idx / (16 * TC), rem = idx - pi * 16 * TC;
+        const int part = first_part + pi;
+        typename W::cell *c0 = wsm + (size_t)part * TR * 16 * TC + rem; // + rr * 16 * TC
+        val v[TR2];
+#pragma unroll
+        for (int rr = 0; rr < TR2; ++rr)
+            v[rr] = W::from_cell(c0[(size_t)rr * 16 * TC]);
+#pragma unroll
+        for (int st = 1; st < TR2; st <<= 1)
+#pragma unroll
+            for (int rr = 0; rr < TR2; ++rr)
+                if (!(rr & st))
+                    W::butterfly(v[rr], v[rr | st]);
+#pragma unroll
+        for (int rr = 0; rr < TR2; ++rr)
+            c0[(size_t)rr * 16 * TC] = W::to_cell(v[rr]);
+    }
+}
+
 // only_if: when not null, the float64 recomputation returns at once unless
 // *only_if is set.
 // BOTH: some chunk of the launch has strings of both #Y parities (two
@@ -305,11 +344,20 @@ __global__ void __launch_bounds__(kWhtThreads, BOTH ? 1 : 2)
     const int RB = n >= 4 ? 16 : (int)D;
     const int64_t nblk = paired ? NB / 2 : NB;
     const int hb = paired ? (63 - __clzll((long long)(xh >> 4))) : 0;
-    const int64_t per = (nblk + n_splits - 1) / n_splits;
+    // rows per split in whole rounds, so that a round's blocks are TR
+    // consecutive, TR-aligned block indices
+    const int64_t per = ((nblk + n_splits - 1) / n_splits + TR - 1) / TR * TR;
     const int64_t b0 = (int64_t)blockIdx.y * per;
     const int64_t b1 = min(nblk, b0 + per);
     const int G = ch.count;
     const bool need_re = ch.n_even > 0, need_im = ch.n_even < G;
+    // two levels: x below the block (x < 16) and 8 row lanes -- the round's 8
+    // blocks differ only in block-index bits 0..2 (row bits 4..6), so a
+    // string's sign over them factors as (-1)^popc(base_0 & z) times the
+    // 8-point Walsh-Hadamard kernel at (z >> 4) & 7: one more 8-point
+    // transform per (coefficient, column) and a round costs each string one
+    // read instead of eight signed adds
+    const bool two_level = !paired && TR == 8;
 
     // chunk strings' z masks in shared memory; this thread owns k = tr + j * TR
     for (int k = tid; k < G; k += blockDim.x)
@@ -376,6 +424,30 @@ __global__ void __launch_bounds__(kWhtThreads, BOTH ? 1 : 2)
         if (tc == 0)
             s_base[tr] = base;
         __syncthreads();
+        if (two_level)
+        {
+            // the parts written above: both, or the one the chunk's strings read
+            wht_rounds<W, 8>(wsm, TR, TC, BOTH ? 0 : (need_re ? 0 : 1), BOTH ? 2 : 1);
+            __syncthreads();
+            const uint64_t base0 = s_base[0];
+#pragma unroll
+            for (int j = 0; j < SLOTS; ++j)
+            {
+                const int k = tr + j * TR;
+                if (k >= G)
+                    break;
+                const uint64_t z = s_z[k];
+                // with one transform (!BOTH) its cells sit in the part the
+                // chunk's strings read
+                const int part = BOTH ? (k >= ch.n_even ? 1 : 0) : (need_re ? 0 : 1);
+                const cell c = wsm[(size_t)(((part * TR + (int)((z >> 4) & 7u)) * 16) + (int)(z & 15u)) * TC + tc];
+                val sum = W::zero();
+                W::add_cell(sum, c, (__popcll(base0 & z) & 1) != 0);
+                W::acc_add(sums[j], sum);
+            }
+            __syncthreads();
+            continue;
+        }
         const int nb = (b1 - mr < (int64_t)TR) ? (int)(b1 - mr) : TR;
         const bool masks = TR <= 32; // one bit per block of the round
         for (int k = tid; masks && k < G; k += blockDim.x)
