@@ -236,26 +236,27 @@ template <typename W> __device__ __forceinline__ void wht16(typename W::val (&v)
 
 // q of the block's 16 rows into vr / vi (one array when !BOTH: each row's
 // single part), the loads of four row pairs issued before any of them is
-// used; for the diagonal group (each row paired with itself) of 8-byte
-// elements eight rows (latency-bound complex64 loads; the 16-byte forms
-// would spill)
+// used; for the diagonal group (each row paired with itself) one load per row,
+// eight rows at a time for 8-byte elements and four for 16-byte ones (eight
+// of those spill)
 template <typename W, bool BOTH>
 __device__ __forceinline__ void rows_q(const typename W::in_t *__restrict__ psi, int64_t S, int64_t t0, uint64_t base,
                                        uint64_t baseB, uint32_t xl, int RB, bool need_re, bool need_im,
                                        typename W::val (&vr)[16], typename W::val (&vi)[16])
 {
-    if (sizeof(typename W::in_t) <= 8 && xl == 0u && baseB == base)
+    if (xl == 0u && baseB == base)
     {
+        constexpr int RGD = sizeof(typename W::in_t) <= 8 ? 8 : 4;
 #pragma unroll
-        for (int r0 = 0; r0 < 16; r0 += 8)
+        for (int r0 = 0; r0 < 16; r0 += RGD)
         {
-            typename W::in_t a[8];
+            typename W::in_t a[RGD];
 #pragma unroll
-            for (int u = 0; u < 8; ++u)
+            for (int u = 0; u < RGD; ++u)
                 if (r0 + u < RB)
                     a[u] = __ldg(psi + (int64_t)(base + r0 + u) * S + t0);
 #pragma unroll
-            for (int u = 0; u < 8; ++u)
+            for (int u = 0; u < RGD; ++u)
                 if (r0 + u < RB)
                     W::qv(a[u], a[u], need_re, need_im, vr[r0 + u], vi[r0 + u]);
         }
