@@ -553,13 +553,17 @@ ExpectPlan plan_expect(const fpg_operator *op, int64_t S, bool fp32, const void 
     const int64_t NB16 = op->n >= 4 ? ((int64_t)1 << (op->n - 4)) : 1;  // 16-row blocks (transform kernel)
     const bool over = column_tile_footprint(p.TC, op->n, p.V * (fp32 ? 8 : 16)) > kColumnTileBytes;
     const bool over1 = column_tile_footprint(p.wht_TC, op->n, fp32 ? 8 : 16) > kColumnTileBytes;
-    // row splits of one launch: enough CTAs for ~8 resident per SM, an L2 row
-    // window when even a one-line column tile does not fit, >= 4 blocks per
-    // row lane
-    auto pick = [](int64_t ctas_per_split, int64_t blocks, int row_lanes, bool windowed, int64_t window) {
+    // row splits of one launch: enough CTAs for kSplitCtasPerSm per SM, an L2
+    // row window when even a one-line column tile does not fit, >= 4 blocks
+    // per row lane.  The double-float kernels are issue-bound and gain from
+    // fewer, longer CTAs (less epilogue and reduction per row); the float32
+    // ones are bound by load latency and gain from more CTAs to pick from
+    constexpr int kSplitCtasPerSmF64 = 4, kSplitCtasPerSmF32 = 24;
+    const int per_sm = fp32 ? kSplitCtasPerSmF32 : kSplitCtasPerSmF64;
+    auto pick = [per_sm](int64_t ctas_per_split, int64_t blocks, int row_lanes, bool windowed, int64_t window) {
         if (ctas_per_split <= 0)
             return 1;
-        const int64_t target = (int64_t)sm_count() * 8;
+        const int64_t target = (int64_t)sm_count() * per_sm;
         int64_t s = (target + ctas_per_split - 1) / ctas_per_split;
         if (windowed)
             s = std::max<int64_t>(s, (blocks + window - 1) / window);
