@@ -84,6 +84,35 @@ __device__ __forceinline__ void df_fma(float xh, float xl, float yh, float yl, f
     sl = __fadd_rn(sl, __fadd_rn(err, e));
 }
 
+// (sh, sl) += (xh + xl) * (yh + yl) for an accumulator whose high part is
+// offset by a power of two sigma that bounds the sum: the caller starts with
+// sh = sigma, sl = 0 and keeps every partial sum and term below sigma / 16 in
+// magnitude, so sh stays inside (sigma / 2, 2 sigma) and on one grid.  Then
+// s - sh is exact (Sterbenz) and one fused multiply-add returns the rounding
+// error of s: 6 float32 operations per term instead of the 12 of df_fma,
+// with the error bounded by ~2^-47 sigma per term rather than by the
+// products.  The caller takes sh - sigma (exact) as the high part of the sum.
+__device__ __forceinline__ void df_fma_offset(float xh, float xl, float yh, float yl, float &sh, float &sl)
+{
+    const float s = __fmaf_rn(xh, yh, sh);
+    const float d = __fsub_rn(s, sh);      // exact
+    const float r = __fmaf_rn(xh, yh, -d); // xh*yh - d = rounding error of s, rounded once
+    sl = __fmaf_rn(xh, yl, sl);
+    sl = __fmaf_rn(xl, yh, sl);
+    sl = __fadd_rn(sl, r);
+    sh = s;
+}
+
+// The offset for df_fma_offset: a power of two > 16 m2 (m2 >= 0 finite), at
+// least 2^-126, so that sums of up to 8 terms of magnitude <= m2 keep the
+// offset accumulator inside its binade pair.  Rounding of 16 * m2 is
+// monotone, so the result also exceeds the exact 16 m2.
+__device__ __forceinline__ float df_offset_for(float m2)
+{
+    const float m16 = __fmul_rn(m2, 16.0f);
+    return __uint_as_float((__float_as_uint(m16) & 0x7f800000u) + 0x00800000u);
+}
+
 // (sh, sl) = (xh + xl) * (yh + yl), to ~2^-47 relative of the product: the
 // first term of a sum, with no addition
 __device__ __forceinline__ void df_mul(float xh, float xl, float yh, float yl, float &sh, float &sl)

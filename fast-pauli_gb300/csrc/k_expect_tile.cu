@@ -22,7 +22,9 @@
 // concurrent CTAs read the same column tile (sized to stay in L2).
 // float32: tile sums in float32, Kahan-compensated across tiles.  float64:
 // double-float (df64.cuh) on the float32 pipes from the split copy of the
-// state (k_df_split), running df64 sums; a value outside the df64 range was
+// state (k_df_split): each tile's sums in offset accumulators (the offset a
+// power of two above 16 times the tile's largest squared high part), their
+// totals into running df64 sums; a value outside the df64 range was
 // flagged by the split, and the pair kernel's float64 form recomputes the
 // groups.  Both sum over the row lanes in double-float pairs and convert
 // only the column totals to float64.
@@ -125,9 +127,23 @@ __device__ __forceinline__ void tile_slot_f32(const float (&rows)[16][2], float 
     }
 }
 
-template <int S_> __device__ __forceinline__ void tile_slot_df(const float (&rows)[16][4], float (&acc)[2][2][2])
+// df64: each of the slot's four sums takes 8 products per tile, all bounded
+// by m^2 (m = the largest high part of the tile's 16 rows), so the tile's
+// sums run in offset accumulators (df_fma_offset, sigma = df_offset_for(m^2))
+// and only their totals go through TwoSum into the running sums
+template <int S_>
+__device__ __forceinline__ void tile_slot_df(const float (&rows)[16][4], float sigma, float (&acc)[2][2][2])
 {
     constexpr int i = kSlotI[S_], j = kSlotJ[S_];
+    float h[2][2], l[2][2];
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+#pragma unroll
+        for (int p = 0; p < 2; ++p)
+        {
+            h[c][p] = sigma;
+            l[c][p] = 0.f;
+        }
 #pragma unroll
     for (int t = 0; t < 16; ++t)
         if (!((t >> j) & 1))
@@ -136,11 +152,16 @@ template <int S_> __device__ __forceinline__ void tile_slot_df(const float (&row
             const int c = (t >> i) & 1;
             const float(&a)[4] = rows[t];
             const float(&b)[4] = rows[u];
-            df_fma(a[0], a[1], b[0], b[1], acc[c][0][0], acc[c][0][1]);
-            df_fma(a[2], a[3], b[2], b[3], acc[c][0][0], acc[c][0][1]);
-            df_fma(a[0], a[1], b[2], b[3], acc[c][1][0], acc[c][1][1]);
-            df_fma(-a[2], -a[3], b[0], b[1], acc[c][1][0], acc[c][1][1]);
+            df_fma_offset(a[0], a[1], b[0], b[1], h[c][0], l[c][0]);
+            df_fma_offset(a[2], a[3], b[2], b[3], h[c][0], l[c][0]);
+            df_fma_offset(a[0], a[1], b[2], b[3], h[c][1], l[c][1]);
+            df_fma_offset(-a[2], -a[3], b[0], b[1], h[c][1], l[c][1]);
         }
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+#pragma unroll
+        for (int p = 0; p < 2; ++p)
+            df_add_lazy(acc[c][p][0], acc[c][p][1], __fsub_rn(h[c][p], sigma), l[c][p]);
 }
 
 // slot S_ of the unit into local accumulator L_, if active
@@ -159,37 +180,44 @@ __device__ __forceinline__ void run_slot(const float (&rows)[16][2], TileAcc<fal
 }
 
 template <int S_, int L_, int NS>
-__device__ __forceinline__ void run_slot(const float (&rows)[16][4], TileAcc<true, NS> &A, int act)
+__device__ __forceinline__ void run_slot(const float (&rows)[16][4], TileAcc<true, NS> &A, int act, float sigma)
 {
     if (!((act >> L_) & 1))
         return;
-    tile_slot_df<S_>(rows, A.run[L_]);
+    tile_slot_df<S_>(rows, sigma, A.run[L_]);
 }
 
-// the NS slots of this CTA: all six, or the half sb / 3
+template <int S_, int L_, int NS>
+__device__ __forceinline__ void run_slot(const float (&rows)[16][2], TileAcc<false, NS> &A, int act, float)
+{
+    run_slot<S_, L_>(rows, A, act);
+}
+
+// the NS slots of this CTA: all six, or the half sb / 3 (sigma: the df64
+// tile offset, unused in float32)
 template <int NS, typename Rows, typename Acc>
-__device__ __forceinline__ void run_slots(const Rows &rows, Acc &A, int act, int sb)
+__device__ __forceinline__ void run_slots(const Rows &rows, Acc &A, int act, int sb, float sigma = 0.f)
 {
     if constexpr (NS == kTileSlots)
     {
-        run_slot<0, 0>(rows, A, act);
-        run_slot<1, 1>(rows, A, act);
-        run_slot<2, 2>(rows, A, act);
-        run_slot<3, 3>(rows, A, act);
-        run_slot<4, 4>(rows, A, act);
-        run_slot<5, 5>(rows, A, act);
+        run_slot<0, 0>(rows, A, act, sigma);
+        run_slot<1, 1>(rows, A, act, sigma);
+        run_slot<2, 2>(rows, A, act, sigma);
+        run_slot<3, 3>(rows, A, act, sigma);
+        run_slot<4, 4>(rows, A, act, sigma);
+        run_slot<5, 5>(rows, A, act, sigma);
     }
     else if (sb == 0)
     {
-        run_slot<0, 0>(rows, A, act);
-        run_slot<1, 1>(rows, A, act);
-        run_slot<2, 2>(rows, A, act);
+        run_slot<0, 0>(rows, A, act, sigma);
+        run_slot<1, 1>(rows, A, act, sigma);
+        run_slot<2, 2>(rows, A, act, sigma);
     }
     else
     {
-        run_slot<3, 0>(rows, A, act);
-        run_slot<4, 1>(rows, A, act);
-        run_slot<5, 2>(rows, A, act);
+        run_slot<3, 0>(rows, A, act, sigma);
+        run_slot<4, 1>(rows, A, act, sigma);
+        run_slot<5, 2>(rows, A, act, sigma);
     }
 }
 
@@ -254,6 +282,7 @@ __global__ void __launch_bounds__(256, kTileMinBlocks<DF, NS>)
             if constexpr (DF)
             {
                 float rows[16][4];
+                float m = 0.f; // largest high part of the tile
 #pragma unroll
                 for (int t = 0; t < 16; ++t)
                 {
@@ -262,9 +291,10 @@ __global__ void __launch_bounds__(256, kTileMinBlocks<DF, NS>)
                     rows[t][1] = v.y;
                     rows[t][2] = v.z;
                     rows[t][3] = v.w;
+                    m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.z)));
                 }
-                run_slots<NS>(rows, A, act, sb);
-                // each sum took 8 df64 terms: renormalise every 4 tiles
+                run_slots<NS>(rows, A, act, sb, df_offset_for(__fmul_rn(m, m)));
+                // each running sum took one tile total: renormalise every 4 tiles
                 if (++since_norm == 4)
                 {
                     since_norm = 0;

@@ -771,3 +771,40 @@ def test_weight2_n14_full_size_properties():
     s = fp.PauliString("XYZI" * 3 + "YZ")
     back = s.apply(s.apply(psi))
     assert normwise(back.cpu().numpy(), psi.cpu().numpy()) < 1e-14
+
+
+def _strings_on_bits(n, xbit, zpairs, xchar="X"):
+    """Strings with `xchar` on row bit xbit and Z on the row bits of each pair
+    (character q acts on row bit n-1-q)."""
+    out = []
+    for a, b in zpairs:
+        s = ["I"] * n
+        s[n - 1 - xbit] = xchar
+        s[n - 1 - a] = "Z"
+        s[n - 1 - b] = "Z"
+        out.append("".join(s))
+    return out
+
+
+@pytest.mark.parametrize("n,xbit", [(6, 1), (6, 5), (10, 1), (10, 3), (10, 6)])
+@pytest.mark.parametrize("S", [5, 40])
+@pytest.mark.parametrize("c64", [False, True])
+def test_transform_kernel_groups_with_two_bit_signs(n, xbit, S, c64):
+    """Groups of >= 10 strings sharing one x whose signs use two row bits go
+    to the transform kernel.  x below the 16-row block (x = 2, 8) with 40
+    states (32 column lanes, 8 row lanes) takes the second level across a
+    round's 8 blocks -- at n = 6 the round holds fewer blocks than that; x =
+    32, 64 pairs blocks and keeps per-block sums; 5 states (8 column lanes,
+    32 row lanes) keep one level.  X and Y on the same bit give both parts."""
+    torch = pytest.importorskip("torch")
+    K = 3
+    rng = np.random.default_rng(50 + 7 * n + xbit + S)
+    pairs = [(a, b) for a in range(n) for b in range(a + 1, n) if xbit not in (a, b)][:20]
+    strings = _strings_on_bits(n, xbit, pairs) + _strings_on_bits(n, xbit, pairs, "Y")
+    P = len(strings)
+    h = (rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))) / np.sqrt(2 * P)
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    want = oracle.summed_expectation(strings, h, psi)
+    states = torch.from_numpy(psi).to(torch.complex64 if c64 else torch.complex128).cuda()
+    got = fp.SummedPauliOp(strings, h).expectation_value(states).cpu().numpy()
+    assert normwise(got, want) < (TOL_MIXED if c64 else TOL_C128)
