@@ -17,10 +17,11 @@ Keys beyond the base contract:
                 fpg_expect_strings, timed alone with CUDA events on its
                 stream) against its binding roof: float32 FMA-pipe issue.  The
                 stage runs its float64 arithmetic as double-float on the
-                float32 pipes; achieved = the stage's float64 operations
-                (fpg_operator_stats: 4 multiply-adds per row visit plus the
-                sign additions) x the float32 instructions each costs in
-                double-float (12 per multiply-add, 8 per addition) / time;
+                float32 pipes; achieved = the stage's float64 operations by
+                kernel family (fpg_operator_family_stats: 4 multiply-adds per
+                row visit plus the sign additions) x the float32 instructions
+                each costs in that family's double-float form (DF64_MULADD_OPS,
+                DF64_ADD_OPS) / time;
                 peak = the float32 FMA rate measured on this GPU
                 (fpg_measure_peak).  "streaming_equiv" keeps the
                 streaming-equivalent HBM figure (16 B per amplitude-term), and
@@ -54,10 +55,18 @@ for _p in (ROOT, PKG):
 
 METRIC = "expval amplitude-terms/s"
 UNIT = "amplitude-terms/s"
-# float32 FMA-pipe instructions of one double-float operation (df64.cuh):
-# a multiply-add (df_fma: 1 multiply, 3 fused multiply-adds, 8 additions) and
-# an addition (df_add_lazy: TwoSum and two additions)
-DF64_FMA_OPS = 12
+# float32 FMA-pipe instructions per double-float operation (df64.cuh), by
+# the kernel family that performs it (fpg_operator_family_stats):
+#  * tile: a product into an offset accumulator (df_fma_offset: 3 fused
+#    multiply-adds, 1 more for the rounding error, 2 additions = 6), plus the
+#    tile total of each sum, 8 products, into the running sum (1 subtraction +
+#    df_add_lazy 8): 6 + 9/8;
+#  * marginal, transform: q = conj(a) b formed as df_mul (4) + df_fma (12) per
+#    two products: 8;
+#  * pair: df_fma, 1 multiply, 3 fused multiply-adds, 8 additions: 12;
+#  * direct: native float64 (the float64 pipe): no float32 operations.
+# An addition is df_add_lazy (TwoSum and two additions): 8.
+DF64_MULADD_OPS = {"tile": 6 + 9 / 8, "marginal": 8, "transform": 8, "pair": 12, "direct": 0}
 DF64_ADD_OPS = 8
 
 
@@ -263,7 +272,9 @@ def run_ours(args, rank, world, dist):
     fp64_rate = _abi.measure_peak(_abi.FPG_C128, stream)  # float64
     nch, visits, adds = op.stats()
     fp64_ops = S * (4 * visits + adds)  # float64 multiply-adds and additions per stage
-    fp32_ops = S * (4 * visits * DF64_FMA_OPS + adds * DF64_ADD_OPS)
+    fam = op.family_stats()
+    fp32_ops = S * sum(4 * v * DF64_MULADD_OPS[f] + (a * DF64_ADD_OPS if DF64_MULADD_OPS[f] else 0)
+                       for f, (v, a) in fam.items())
     alg_bytes_expect = terms * 16
     traffic = _ncu_traffic("expect_stage_n14_weight2_fp64.md")
     roof = {
@@ -277,10 +288,13 @@ def run_ours(args, rank, world, dist):
                   "+ family reductions)",
         "kernel_ms": t_expect * 1e3,
         "ops_per_launch": fp32_ops,
-        "model": "float64 operations of the stage (fpg_operator_stats: 4 multiply-adds per row visit + sign "
-                 "additions) x float32 instructions per double-float operation (12 per multiply-add, 8 per "
-                 "addition); an upper estimate (the marginal and transform kernels form each first product "
-                 "without an addition)",
+        "model": "float64 operations of the stage by kernel family (fpg_operator_family_stats: 4 multiply-adds "
+                 "per row visit + sign additions) x the float32 instructions that family spends per double-float "
+                 "operation: multiply-add 7.125 in the tile kernel (offset accumulators, 6, and the tile "
+                 "totals), 8 in the marginal and transform kernels, 12 in the pair kernel; addition 8. "
+                 "Loads, index arithmetic, tile maxima and renormalisations are not counted",
+        "ops_by_family": {f: S * (4 * v * DF64_MULADD_OPS[f] + (a * DF64_ADD_OPS if DF64_MULADD_OPS[f] else 0))
+                          for f, (v, a) in fam.items() if v},
         "traffic": traffic,
         "traffic_source": "ncu DRAM bytes of one stage launch, profiles/expect_stage_n14_weight2_fp64.md "
                           "(captured once, not in this run)",
@@ -328,8 +342,8 @@ def run_ours(args, rank, world, dist):
                "h2d_bytes_per_step": D * S * 16 + P * K * 16, "d2h_bytes_per_step": K * S * 16,
                "ms_per_call": t_pg * 1e3,
                "api": "fast_pauli.SummedPauliOp.expectation_value(numpy array in ordinary pageable host memory)",
-               "overlap": "two column chunks, the first a quarter of the states: the rest is copied in while the "
-                          "first is computed",
+               "overlap": "three column chunks of 128, 448 and 448 states: each chunk is copied in while the one "
+                          "before it is computed",
                "max_rel_err_vs_device_path": err_pg,
                "pinned": {"value": world * terms / t_pn, "unit": UNIT, "ms_per_call": t_pn * 1e3,
                           "api": "fast_pauli.SummedPauliOp.expectation_value(numpy array in pinned host memory)",

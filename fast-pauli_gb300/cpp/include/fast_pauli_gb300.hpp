@@ -295,12 +295,11 @@ struct Event
     }
 };
 
-// Column chunks of a call whose states are `bytes` of pinned host memory in
-// S columns: chunk c + 1 is copied in while chunk c is computed (columns are
-// independent).  Two by default (a narrower call costs a little more per
-// column, so more chunks hide less than they add); one (no overlap) below
-// 64 MiB or 256 columns; the environment variable FPG_HOST_CHUNKS overrides
-// the count.
+// Column chunks of a call whose states are `bytes` of host memory in S
+// columns: chunk c + 1 is copied in while chunk c is computed (columns are
+// independent).  A narrower call costs more per column, so few chunks: three
+// from 256 MiB and 512 columns, two from 64 MiB and 256 columns, else one
+// (no overlap); the environment variable FPG_HOST_CHUNKS overrides the count.
 inline size_t host_column_chunks(size_t S, size_t bytes)
 {
     const size_t most = std::max<size_t>(1, S / 64);
@@ -312,6 +311,8 @@ inline size_t host_column_chunks(size_t S, size_t bytes)
     }
     if (bytes < (size_t(64) << 20) || S < 256)
         return 1;
+    if (bytes >= (size_t(256) << 20) && S >= 512)
+        return std::min<size_t>(3, most);
     return std::min<size_t>(2, most);
 }
 
@@ -1322,15 +1323,20 @@ template <std::floating_point T> struct SummedPauliOp
                                cudaStream_t st) const
     {
         const size_t D = dim(), K = n_operators(), el = sizeof(C);
-        // widths in multiples of 64 columns: the first about a quarter of S
-        // (its computation then takes about as long as the copy of the rest,
-        // a narrower call costing a little more per column), the rest split
-        // evenly, the remainder in the last chunk
+        // widths in multiples of 64 columns: the first small, a quarter of S
+        // with two chunks and an eighth with more (its copy is the part that
+        // nothing hides; its computation then takes about as long as the
+        // next chunk's copy), the rest split evenly, the remainder in the last
+        // chunk.  n=14 weight<=2 workload, 1024 columns, pageable states:
+        // 4.17 ms without chunks, 3.65 ms in two (a quarter first), 3.55 ms
+        // in three (an eighth first); 3.72 / 3.75 ms for three / four with a
+        // quarter first, 3.72 / 3.88 ms for four / five with an eighth
         std::vector<size_t> c0, cw;
         size_t left = S;
+        const size_t first = nc > 2 ? S / 8 : S / 4;
         for (size_t c = 0; c < nc && left; ++c)
         {
-            size_t w = c == 0 ? std::max<size_t>(64, S / 4 / 64 * 64)
+            size_t w = c == 0 ? std::max<size_t>(64, first / 64 * 64)
                               : std::max<size_t>(64, left / (nc - c) / 64 * 64);
             w = c + 1 == nc ? left : std::min(w, left);
             c0.push_back(S - left);

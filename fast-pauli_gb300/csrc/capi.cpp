@@ -1053,44 +1053,57 @@ extern "C"
         return FPG_OK;
     }
 
-    int fpg_operator_stats(const fpg_operator *op, int64_t *n_chunks, int64_t *row_visits, int64_t *sign_adds)
+    int fpg_operator_family_stats(const fpg_operator *op, int64_t *row_visits, int64_t *sign_adds)
     {
-        if (!op)
-            return set_error(FPG_ERR_INVALID, "op is null");
-        // the per-call decomposition: direct chunks + transform chunks
+        if (!op || !row_visits || !sign_adds)
+            return set_error(FPG_ERR_INVALID, "null argument");
+        // the per-call decomposition, by kernel family
         const int64_t D = (int64_t)1 << op->n;
-        int64_t visits = 0, adds = 0;
+        for (int f = 0; f < FPG_FAMILY_COUNT; ++f)
+            row_visits[f] = sign_adds[f] = 0;
         for (int c = 0; c < kNumChunkClasses; ++c)
             for (int i = op->fast_class_begin[(size_t)c]; i < op->fast_class_begin[(size_t)c + 1]; ++i)
             {
                 const bool paired = (op->fast_chunks[(size_t)i].x >> 5) != 0;
                 const int64_t rows = paired ? D / 2 : D;
-                visits += rows;
-                adds += rows * (kChunkClasses[c].ge + kChunkClasses[c].go);
+                row_visits[FPG_FAMILY_DIRECT] += rows;
+                sign_adds[FPG_FAMILY_DIRECT] += rows * (kChunkClasses[c].ge + kChunkClasses[c].go);
             }
         for (const WhtChunk &w : op->wht)
         {
             const bool paired = (w.x >> 4) != 0;
             const int64_t rows = paired ? D / 2 : D;
             const int parts = (w.n_even > 0 ? 1 : 0) + (w.n_even < w.count ? 1 : 0);
-            visits += rows;
+            row_visits[FPG_FAMILY_TRANSFORM] += rows;
             // 16-point transform: 4 adds per row per part; one add per string per 16 rows
-            adds += rows * 4 * parts + (rows / 16) * w.count;
+            sign_adds[FPG_FAMILY_TRANSFORM] += rows * 4 * parts + (rows / 16) * w.count;
         }
-        std::vector<PairChunk> all_pairs(op->pairs);
-        all_pairs.insert(all_pairs.end(), op->tile_pairs.begin(), op->tile_pairs.end());
-        for (const PairChunk &pc : all_pairs)
-        {
-            const bool paired = pc.x != 0; // rows paired across or inside 32-row blocks
-            const int64_t rows = paired ? D / 2 : D;
-            visits += rows; // four FMAs per row, the running sums included: no sign adds
-        }
+        // four FMAs per row, the running sums included: no sign adds
+        for (const PairChunk &pc : op->pairs)
+            row_visits[FPG_FAMILY_PAIR] += pc.x != 0 ? D / 2 : D; // rows paired across or inside 32-row blocks
+        for (const PairChunk &pc : op->tile_pairs)
+            row_visits[FPG_FAMILY_TILE] += pc.x != 0 ? D / 2 : D;
         for (const MargChunk &mc : op->margs)
         {
             const int64_t rows = mc.x != 0 ? D / 2 : D;
             const int parts = ((mc.flags & 1) ? 1 : 0) + ((mc.flags & 2) ? 1 : 0);
-            visits += rows;
-            adds += rows * parts * 17 / 8; // marginal tree: 68 adds per 32 rows and part
+            row_visits[FPG_FAMILY_MARGINAL] += rows;
+            sign_adds[FPG_FAMILY_MARGINAL] += rows * parts * 17 / 8; // marginal tree: 68 adds per 32 rows and part
+        }
+        return FPG_OK;
+    }
+
+    int fpg_operator_stats(const fpg_operator *op, int64_t *n_chunks, int64_t *row_visits, int64_t *sign_adds)
+    {
+        if (!op)
+            return set_error(FPG_ERR_INVALID, "op is null");
+        int64_t v[FPG_FAMILY_COUNT], a[FPG_FAMILY_COUNT];
+        fpg_operator_family_stats(op, v, a);
+        int64_t visits = 0, adds = 0;
+        for (int f = 0; f < FPG_FAMILY_COUNT; ++f)
+        {
+            visits += v[f];
+            adds += a[f];
         }
         if (n_chunks)
             *n_chunks = (int64_t)(op->fast_chunks.size() + op->wht.size() + op->pairs.size() + op->tiles.size() +

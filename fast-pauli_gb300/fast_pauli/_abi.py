@@ -49,6 +49,7 @@ SIGNATURES = {
     "fpg_operator_destroy": (ctypes.c_int, [_P]),
     "fpg_operator_info": (ctypes.c_int, [_P, _PI32, _PI64, _PI64]),
     "fpg_operator_stats": (ctypes.c_int, [_P, _PI64, _PI64, _PI64]),
+    "fpg_operator_family_stats": (ctypes.c_int, [_P, _PI64, _PI64]),
     "fpg_sparse_repr": (ctypes.c_int, [ctypes.c_char_p, _I32, _P, _P, _P]),
     "fpg_apply": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I32, _P]),
     "fpg_expect_strings": (ctypes.c_int, [_P, _P, _P, _I64, _I32, _P]),
@@ -186,6 +187,15 @@ class Operator:
         a = ctypes.c_int64()
         check(lib().fpg_operator_stats(self._h, ctypes.byref(c), ctypes.byref(v), ctypes.byref(a)))
         return c.value, v.value, a.value
+
+    FAMILIES = ("direct", "transform", "pair", "marginal", "tile")
+
+    def family_stats(self) -> dict[str, tuple[int, int]]:
+        """{family: (row visits per column, signed accumulations per column)}."""
+        v = (ctypes.c_int64 * len(self.FAMILIES))()
+        a = (ctypes.c_int64 * len(self.FAMILIES))()
+        check(lib().fpg_operator_family_stats(self._h, v, a))
+        return {f: (v[i], a[i]) for i, f in enumerate(self.FAMILIES)}
 
     def close(self) -> None:
         if self._h:

@@ -126,6 +126,24 @@ int fpg_operator_info(const fpg_operator *op, int32_t *n_qubits, int64_t *n_stri
 int fpg_operator_stats(const fpg_operator *op, int64_t *n_chunks, int64_t *row_visits, int64_t *sign_adds);
 
 /*
+ * The same work split by the kernel family that does it: row_visits[f] and
+ * sign_adds[f] for f in FPG_FAMILY_DIRECT .. FPG_FAMILY_TILE (arrays of
+ * FPG_FAMILY_COUNT entries).  The families compute with different float32
+ * costs per float64 operation in the df64 form, which bench.py's roofline
+ * counts.  No counterpart in the reference.
+ */
+enum
+{
+    FPG_FAMILY_DIRECT = 0,    /* direct-kernel chunks */
+    FPG_FAMILY_TRANSFORM = 1, /* 16-point Walsh-Hadamard transform kernel */
+    FPG_FAMILY_PAIR = 2,      /* pair kernel */
+    FPG_FAMILY_MARGINAL = 3,  /* marginal kernel */
+    FPG_FAMILY_TILE = 4,      /* tile kernel (two-position groups, four row bits per unit) */
+    FPG_FAMILY_COUNT = 5
+};
+int fpg_operator_family_stats(const fpg_operator *op, int64_t *row_visits, int64_t *sign_adds);
+
+/*
  * Sparse pattern of one Pauli string on the device: cols[i] = column of the
  * non-zero in row i, vals[i] = its value (complex128 interleaved), i < 2^n.
  * Bit-exact replacement for get_sparse_repr<double>

@@ -808,3 +808,27 @@ def test_transform_kernel_groups_with_two_bit_signs(n, xbit, S, c64):
     states = torch.from_numpy(psi).to(torch.complex64 if c64 else torch.complex128).cuda()
     got = fp.SummedPauliOp(strings, h).expectation_value(states).cpu().numpy()
     assert normwise(got, want) < (TOL_MIXED if c64 else TOL_C128)
+
+
+def test_family_stats_partition_the_operator_work():
+    """fpg_operator_family_stats splits fpg_operator_stats' work by kernel
+    family; for the 861 weight <= 2 strings at n = 14 the 91 two-position
+    groups are the tile kernel's, the 14 one-position groups the marginal
+    kernel's and the diagonal group (I, Z, ZZ) the transform kernel's."""
+    from fast_pauli import _abi
+
+    n = 14
+    strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
+    op = _abi.Operator(strings)
+    try:
+        _, visits, adds = op.stats()
+        fam = op.family_stats()
+    finally:
+        op.close()
+    assert sum(v for v, _ in fam.values()) == visits
+    assert sum(a for _, a in fam.values()) == adds
+    half = 1 << (n - 1)
+    assert fam["tile"] == (91 * half, 0)
+    assert fam["marginal"][0] == 14 * half
+    assert fam["transform"][0] == 1 << n
+    assert fam["pair"] == (0, 0) and fam["direct"] == (0, 0)
