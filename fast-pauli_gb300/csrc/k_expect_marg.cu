@@ -112,6 +112,9 @@ struct ArF32
     }
     // small elements: a block half's 32 loads are issued before any use
     static constexpr int kPrefetchRows = 16;
+    // row offsets from the CTA's table (the df64 form spilled with it and
+    // ran 1.04x slower; this form went 2.56 -> 1.92 ms per n=18 launch)
+    static constexpr bool kRowTable = true;
     using raw_t = float2;
     static __device__ __forceinline__ raw_t ld(const in_t *psi, int64_t e)
     {
@@ -137,6 +140,7 @@ struct ArF64
     using in_t = double;
     static constexpr bool kRaises = false, kRecompute = true;
     static constexpr int kPrefetchRows = 0;
+    static constexpr bool kRowTable = false;
     using raw_t = double2;
     static __device__ __forceinline__ raw_t ld(const in_t *, int64_t)
     {
@@ -210,6 +214,7 @@ struct ArDF
     using in_t = double;
     static constexpr bool kRaises = true, kRecompute = false;
     static constexpr int kPrefetchRows = 0;
+    static constexpr bool kRowTable = false;
     using raw_t = float4;
     static __device__ __forceinline__ float4 raw_zero()
     {
@@ -313,13 +318,24 @@ struct ArDFS : ArDF
 // Sums of one block: bt[part] (total) and bl[part][j] (rows whose visited-row
 // bit j is set).  LB = 5: all 32 rows, visited bit j = row bit j.  LB = 4:
 // the 16 rows with bit pl clear; visited bit j = row bit (j < pl ? j : j + 1).
-template <typename A, int LB>
+// TAB (the float32 policy, n >= 5, 32 S < 2^31): the element offsets of
+// the visited rows from the block's first row come from the CTA's table
+// s_rows ({row, partner row} x S, 32-bit), so a row load is one wide
+// multiply-add on a pointer formed once per block instead of 64-bit index
+// arithmetic per row.
+template <typename A, int LB, bool TAB>
 __device__ __forceinline__ void block_marginals(const typename A::in_t *__restrict__ psi, int64_t S, int64_t t0,
                                                 uint64_t base, uint64_t baseB, uint32_t xl, int pl, int RB,
                                                 bool need_re, bool need_im, typename A::val (&bt)[2],
-                                                typename A::val (&bl)[2][5], bool &bad)
+                                                typename A::val (&bl)[2][5], bool &bad, const int2 *s_rows)
 {
     using val = typename A::val;
+    [[maybe_unused]] const typename A::raw_t *qa = nullptr, *qb = nullptr;
+    if constexpr (TAB)
+    {
+        qa = reinterpret_cast<const typename A::raw_t *>(psi) + ((int64_t)base * S + t0);
+        qb = reinterpret_cast<const typename A::raw_t *>(psi) + ((int64_t)baseB * S + t0);
+    }
     // 16 visited rows at a time (LB = 5: two halves, bit 4 from the half)
 #pragma unroll 1
     for (int h = 0; h < (1 << (LB - 4)); ++h)
@@ -342,7 +358,14 @@ __device__ __forceinline__ void block_marginals(const typename A::in_t *__restri
                 if ((4 * k) % PF == 0)
                 {
 #pragma unroll
-                    for (int j = 0; j < PF; ++j)
+                    for (int j = 0; TAB && j < PF; ++j)
+                    {
+                        const int2 o = s_rows[16 * h + 4 * k + j];
+                        ra[j] = __ldg(qa + o.x);
+                        rb[j] = __ldg(qb + o.y);
+                    }
+#pragma unroll
+                    for (int j = 0; !TAB && j < PF; ++j)
                     {
                         const uint32_t m2 = (uint32_t)(16 * h + 4 * k + j);
                         const uint32_t r = LB == 5 ? m2 : (((m2 >> pl) << (pl + 1)) | (m2 & ((1u << pl) - 1u)));
@@ -417,7 +440,7 @@ __device__ __forceinline__ void block_marginals(const typename A::in_t *__restri
 
 // range_flag: ArDF raises it for inputs outside the df64 range; ArF64 (the
 // recomputation launched after it) returns at once unless it is set.
-template <typename A, int NH>
+template <typename A, int NH, bool TAB>
 __global__ void __launch_bounds__(256, 2)
     k_expect_marg(const typename A::in_t *__restrict__ psi, int64_t S, int n, const StringRec *__restrict__ recs,
                   const int32_t *__restrict__ orig, int64_t P, const MargChunk *__restrict__ chunks, int TC,
@@ -463,6 +486,19 @@ __global__ void __launch_bounds__(256, 2)
     const uint64_t hmask = ch.zmask & ~31ull;
     for (int j = 0; j < 2 * NH; ++j)
         smh[j * 256 + tid] = make_float2(0.f, 0.f);
+    // visited row m2 -> element offsets of its row and partner row from the
+    // block's first rows (base, baseB)
+    __shared__ int2 s_rows[32];
+    if constexpr (TAB)
+    {
+        if (tid < 32)
+        {
+            const uint32_t m2 = (uint32_t)tid;
+            const uint32_t r = pl < 0 ? m2 : (((m2 >> pl) << (pl + 1)) | (m2 & ((1u << pl) - 1u)));
+            s_rows[tid] = make_int2((int)(r & 31u) * (int)S, (int)((r ^ xl) & 31u) * (int)S);
+        }
+        __syncthreads();
+    }
 
     acc tot[2], ml[2][5];
 #pragma unroll
@@ -520,9 +556,11 @@ __global__ void __launch_bounds__(256, 2)
                 for (int j = 0; j < 5; ++j)
                     bl[p][j] = A::zero();
             if (pl < 0)
-                block_marginals<A, 5>(psi, S, t0, base, baseB, xl, pl, RB, need_re, need_im, bt, bl, bad);
+                block_marginals<A, 5, TAB>(psi, S, t0, base, baseB, xl, pl, RB, need_re, need_im, bt, bl, bad,
+                                           s_rows);
             else
-                block_marginals<A, 4>(psi, S, t0, base, baseB, xl, pl, RB, need_re, need_im, bt, bl, bad);
+                block_marginals<A, 4, TAB>(psi, S, t0, base, baseB, xl, pl, RB, need_re, need_im, bt, bl, bad,
+                                           s_rows);
             const uint64_t hi = base & hi_mask;
             if (in_run && hi != run_hi)
             {
@@ -663,19 +701,35 @@ __global__ void __launch_bounds__(256, 2)
     }
 }
 
-template <typename A, int NH>
-cudaError_t launch_nh(const void *psi, int64_t S, int n, const DevOp &op, const MargChunk *d_chunks, int n_chunks,
-                      int TC, int n_ctiles, int n_splits, double *out, int *range_flag, cudaStream_t st)
+template <typename A, int NH, bool TAB>
+cudaError_t launch_nh_tab(const void *psi, int64_t S, int n, const DevOp &op, const MargChunk *d_chunks,
+                          int n_chunks, int TC, int n_ctiles, int n_splits, double *out, int *range_flag,
+                          cudaStream_t st)
 {
     constexpr int NV = 2 * (1 + 5 + NH);
     const size_t smem = (size_t)(8 * 256 + NV * TC) * sizeof(double) + (size_t)2 * NH * 256 * sizeof(float2);
     dim3 grid((unsigned)n_chunks, (unsigned)n_splits, (unsigned)n_ctiles);
-    cudaError_t e = cudaFuncSetAttribute(k_expect_marg<A, NH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_expect_marg<A, NH, TAB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
-    k_expect_marg<A, NH><<<grid, 256, smem, st>>>((const typename A::in_t *)psi, S, n, op.recs, op.orig, op.P,
-                                                  d_chunks, TC, n_splits, out, range_flag);
+    k_expect_marg<A, NH, TAB><<<grid, 256, smem, st>>>((const typename A::in_t *)psi, S, n, op.recs, op.orig, op.P,
+                                                       d_chunks, TC, n_splits, out, range_flag);
     return launched();
+}
+
+template <typename A, int NH>
+cudaError_t launch_nh(const void *psi, int64_t S, int n, const DevOp &op, const MargChunk *d_chunks, int n_chunks,
+                      int TC, int n_ctiles, int n_splits, double *out, int *range_flag, cudaStream_t st)
+{
+    // the offset table: the policies that use it, whole 32-row blocks, and
+    // offsets 31 S that fit 32 bits
+    if constexpr (A::kRowTable)
+        if (n >= 5 && 32 * S < ((int64_t)1 << 31))
+            return launch_nh_tab<A, NH, true>(psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out,
+                                              range_flag, st);
+    return launch_nh_tab<A, NH, false>(psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, range_flag,
+                                       st);
 }
 
 template <int NH>

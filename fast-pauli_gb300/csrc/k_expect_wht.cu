@@ -26,6 +26,8 @@
 // double-float (df64.cuh) on the float32 pipes, the state split once per call
 // (k_df_split), followed by the float64 form, which recomputes only when the
 // call's range flag was raised.
+#include <type_traits>
+
 #include "common.cuh"
 #include "df64.cuh"
 
@@ -238,12 +240,51 @@ template <typename W> __device__ __forceinline__ void wht16(typename W::val (&v)
 // single part), the loads of four row pairs issued before any of them is
 // used; for the diagonal group (each row paired with itself) one load per row,
 // eight rows at a time for 8-byte elements and four for 16-byte ones (eight
-// of those spill)
-template <typename W, bool BOTH>
+// of those spill).  OFF32 (n >= 4, 16 S < 2^31): row r of a block is loaded
+// at the block's first element plus r S in 32 bits, one wide multiply-add
+// per load, instead of 64-bit index arithmetic per row.
+template <typename W, bool BOTH, bool OFF32>
 __device__ __forceinline__ void rows_q(const typename W::in_t *__restrict__ psi, int64_t S, int64_t t0, uint64_t base,
                                        uint64_t baseB, uint32_t xl, int RB, bool need_re, bool need_im,
                                        typename W::val (&vr)[16], typename W::val (&vi)[16])
 {
+    if constexpr (OFF32)
+    {
+        const int S32 = (int)S;
+        const typename W::in_t *qa = psi + ((int64_t)base * S + t0);
+        if (xl == 0u && baseB == base)
+        {
+            constexpr int RGD = sizeof(typename W::in_t) <= 8 ? 8 : 4;
+#pragma unroll
+            for (int r0 = 0; r0 < 16; r0 += RGD)
+            {
+                typename W::in_t a[RGD];
+#pragma unroll
+                for (int u = 0; u < RGD; ++u)
+                    a[u] = __ldg(qa + (r0 + u) * S32);
+#pragma unroll
+                for (int u = 0; u < RGD; ++u)
+                    W::qv(a[u], a[u], need_re, need_im, vr[r0 + u], vi[r0 + u]);
+            }
+            return;
+        }
+        const typename W::in_t *qb = psi + ((int64_t)baseB * S + t0);
+#pragma unroll
+        for (int r0 = 0; r0 < 16; r0 += 4)
+        {
+            typename W::in_t a[4], b[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+            {
+                a[u] = __ldg(qa + (r0 + u) * S32);
+                b[u] = __ldg(qb + (int)((uint32_t)(r0 + u) ^ xl) * S32);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                W::qv(a[u], b[u], need_re, need_im, vr[r0 + u], vi[r0 + u]);
+        }
+        return;
+    }
     if (xl == 0u && baseB == base)
     {
         constexpr int RGD = sizeof(typename W::in_t) <= 8 ? 8 : 4;
@@ -311,7 +352,7 @@ __device__ __forceinline__ void wht_rounds(typename W::cell *wsm, int TR, int TC
 // *only_if is set.
 // BOTH: some chunk of the launch has strings of both #Y parities (two
 // transforms per block); otherwise one.
-template <typename W, int SLOTS, bool BOTH>
+template <typename W, int SLOTS, bool BOTH, bool OFF32>
 __global__ void __launch_bounds__(kWhtThreads, BOTH ? 1 : 2)
     k_expect_wht(const typename W::in_t *__restrict__ psi, int64_t S, int n, const StringRec *__restrict__ recs,
                  const int32_t *__restrict__ orig, int64_t P, const WhtChunk *__restrict__ chunks, int TC,
@@ -393,7 +434,7 @@ __global__ void __launch_bounds__(kWhtThreads, BOTH ? 1 : 2)
                 vim[r] = W::zero();
             }
             if (have && col_ok)
-                rows_q<W, true>(psi, S, t0, base, baseB, xl, RB, need_re, need_im, vre, vim);
+                rows_q<W, true, OFF32>(psi, S, t0, base, baseB, xl, RB, need_re, need_im, vre, vim);
             if (need_re)
                 wht16<W>(vre);
             if (need_im)
@@ -415,7 +456,7 @@ __global__ void __launch_bounds__(kWhtThreads, BOTH ? 1 : 2)
             for (int r = 0; r < 16; ++r)
                 v[r] = W::zero();
             if (have && col_ok)
-                rows_q<W, false>(psi, S, t0, base, baseB, xl, RB, need_re, need_im, v, v);
+                rows_q<W, false, OFF32>(psi, S, t0, base, baseB, xl, RB, need_re, need_im, v, v);
             wht16<W>(v);
             cell *w = need_re ? w0 : w1;
 #pragma unroll
@@ -494,18 +535,32 @@ __global__ void __launch_bounds__(kWhtThreads, BOTH ? 1 : 2)
     }
 }
 
+template <typename W, int SL, bool BOTH, bool OFF32>
+cudaError_t launch_w_off(const void *psi, int64_t S, int n, const DevOp &op, const WhtChunk *d_chunks, int n_chunks,
+                         int TC, int n_ctiles, int n_splits, double *out, const int *only_if, size_t smem,
+                         cudaStream_t st)
+{
+    dim3 grid((unsigned)n_chunks, (unsigned)n_splits, (unsigned)n_ctiles);
+    cudaError_t e = cudaFuncSetAttribute(k_expect_wht<W, SL, BOTH, OFF32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    k_expect_wht<W, SL, BOTH, OFF32><<<grid, kWhtThreads, smem, st>>>(
+        (const typename W::in_t *)psi, S, n, op.recs, op.orig, op.P, d_chunks, TC, n_splits, out, only_if);
+    return launched();
+}
+
+// 32-bit row offsets for the float32 form (W32) of whole 16-row blocks
 template <typename W, int SL, bool BOTH>
 cudaError_t launch_w(const void *psi, int64_t S, int n, const DevOp &op, const WhtChunk *d_chunks, int n_chunks,
                      int TC, int n_ctiles, int n_splits, double *out, const int *only_if, size_t smem, cudaStream_t st)
 {
-    dim3 grid((unsigned)n_chunks, (unsigned)n_splits, (unsigned)n_ctiles);
-    cudaError_t e =
-        cudaFuncSetAttribute(k_expect_wht<W, SL, BOTH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess)
-        return e;
-    k_expect_wht<W, SL, BOTH><<<grid, kWhtThreads, smem, st>>>((const typename W::in_t *)psi, S, n, op.recs, op.orig,
-                                                               op.P, d_chunks, TC, n_splits, out, only_if);
-    return launched();
+    if constexpr (std::is_same_v<W, W32>)
+        if (n >= 4 && 16 * S < ((int64_t)1 << 31))
+            return launch_w_off<W, SL, BOTH, true>(psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out,
+                                                   only_if, smem, st);
+    return launch_w_off<W, SL, BOTH, false>(psi, S, n, op, d_chunks, n_chunks, TC, n_ctiles, n_splits, out, only_if,
+                                            smem, st);
 }
 
 template <int SL, bool BOTH>
