@@ -226,8 +226,8 @@ template <bool DF, int NS> constexpr int kTileMinBlocks = DF ? (NS == kTileSlots
 // DF: psi = the df64 split copy (float4 per element); else float2 elements.
 // NS = 6: one CTA per unit; NS = 3: two CTAs per unit (blockIdx.x = 2 unit +
 // half), each with half the slots and half the accumulator registers.
-// OFF32: 2^n x S < 2^31, so that the tile rows' offsets from the tile's
-// first row fit 32 bits (one wide multiply-add per row load)
+// OFF32: 2^n x S < 2^31, so that the tile's first row and element index and
+// the rows' offsets from it fit 32 bits (one wide multiply-add per row load)
 template <bool DF, int NS, bool OFF32>
 __global__ void __launch_bounds__(256, kTileMinBlocks<DF, NS>)
     k_expect_tile(const void *__restrict__ psi, int64_t S, int n, const StringRec *__restrict__ recs,
@@ -270,13 +270,27 @@ __global__ void __launch_bounds__(256, kTileMinBlocks<DF, NS>)
         [[maybe_unused]] int since_norm = 0;
         for (int64_t m = b0 + tr; m < b1; m += TR)
         {
-            // base: m with zero bits inserted at q0 < q1 < q2 < q3
-            uint64_t base = (uint64_t)m;
-            base = ((base >> q0) << (q0 + 1)) | (base & ((1ull << q0) - 1ull));
-            base = ((base >> q1) << (q1 + 1)) | (base & ((1ull << q1) - 1ull));
-            base = ((base >> q2) << (q2 + 1)) | (base & ((1ull << q2) - 1ull));
-            base = ((base >> q3) << (q3 + 1)) | (base & ((1ull << q3) - 1ull));
-            const int64_t e0 = (int64_t)base * S + t0;
+            // base: m with zero bits inserted at q0 < q1 < q2 < q3 (OFF32:
+            // 2^n S < 2^31, so the row index and the element index fit 32 bits)
+            int64_t e0;
+            if constexpr (OFF32)
+            {
+                uint32_t b = (uint32_t)m;
+                b = ((b >> q0) << (q0 + 1)) | (b & ((1u << q0) - 1u));
+                b = ((b >> q1) << (q1 + 1)) | (b & ((1u << q1) - 1u));
+                b = ((b >> q2) << (q2 + 1)) | (b & ((1u << q2) - 1u));
+                b = ((b >> q3) << (q3 + 1)) | (b & ((1u << q3) - 1u));
+                e0 = (int32_t)b * (int32_t)S + (int32_t)t0;
+            }
+            else
+            {
+                uint64_t base = (uint64_t)m;
+                base = ((base >> q0) << (q0 + 1)) | (base & ((1ull << q0) - 1ull));
+                base = ((base >> q1) << (q1 + 1)) | (base & ((1ull << q1) - 1ull));
+                base = ((base >> q2) << (q2 + 1)) | (base & ((1ull << q2) - 1ull));
+                base = ((base >> q3) << (q3 + 1)) | (base & ((1ull << q3) - 1ull));
+                e0 = (int64_t)base * S + t0;
+            }
             const float4 *row4 = reinterpret_cast<const float4 *>(psi) + e0;
             const float2 *row2 = reinterpret_cast<const float2 *>(psi) + e0;
             if constexpr (DF)
@@ -383,10 +397,11 @@ template <bool DF, int NS>
 cudaError_t launch_tile(const void *psi, int64_t S, int n, const DevOp &op, const TileChunk *d_units, int n_units,
                         int TC, int n_ctiles, int n_splits, double *out, cudaStream_t st)
 {
-    // float64 only: the step of the n=14 weight<=2 workload 2.92 -> 2.80 ms;
-    // the complex64 form measured 8.5 -> 8.8 ms at n=18 with it
-    if constexpr (DF)
-        if ((((int64_t)1 << n) * S) < ((int64_t)1 << 31))
+    // 32-bit row offsets and row index: the float64 step of the n=14
+    // weight<=2 workload 2.92 -> 2.80 ms; the complex64 form at n=18 once
+    // measured 8.5 -> 8.8 ms with 32-bit offsets alone, and 7.15 -> 7.09 ms
+    // with the 32-bit row index added
+    if ((((int64_t)1 << n) * S) < ((int64_t)1 << 31))
             return launch_tile<DF, NS, true>(psi, S, n, op, d_units, n_units, TC, n_ctiles, n_splits, out, st);
     return launch_tile<DF, NS, false>(psi, S, n, op, d_units, n_units, TC, n_ctiles, n_splits, out, st);
 }
