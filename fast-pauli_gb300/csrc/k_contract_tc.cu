@@ -11,7 +11,9 @@
 // x_hi = tf32(x) (round to nearest) and x_lo = tf32(x - x_hi); the product is
 // A_hi B_hi + A_hi B_lo + A_lo B_hi, accumulated in float32 in TMEM over one
 // 32-deep k segment per CTA (grid z = segment); the finishing kernels sum the
-// segments in float64.  Long float32 accumulations over thousands of terms
+// segments in double-float on the float32 pipes (TwoSum: ~2^-48 of the sum of
+// their magnitudes, far below the complex64 output's rounding).  Long float32
+// accumulations over thousands of terms
 // with cancellation (e.g. a PauliOp with 4096 strings, K = 1) otherwise lose
 // ~1e-5 relative accuracy.
 //
@@ -200,7 +202,7 @@ __global__ void k_prep_b_weighted(const float *__restrict__ X, int64_t K, int64_
 // One 128x128 tile of one k segment per CTA (blockIdx.z = segment of
 // seg_chunks 32-deep chunks): C[z] (rows_pad x cols_pad, row-major float32)
 // = A B^T restricted to the segment.  Accumulation is float32 inside a
-// segment only; the segments are summed in float64 by the finishing kernels.
+// segment only; the finishing kernels sum the segments in double-float.
 __global__ void __launch_bounds__(128, 1)
     k_gemm_tf32x3(const float *__restrict__ a_hi, const float *__restrict__ a_lo, const float *__restrict__ b_hi,
                   const float *__restrict__ b_lo, int64_t kchunks, int64_t seg_chunks, int64_t rows_pad,
@@ -354,13 +356,25 @@ __global__ void __launch_bounds__(128, 1)
 }
 
 // -------------------------------------------------------------- epilogues
-// Segments are summed in float64, in segment order.
-__device__ __forceinline__ double seg_sum(const float *__restrict__ C, int64_t nseg, int64_t seg_stride, int64_t idx)
+// start + the segments' values at idx, in segment order, as an unevaluated
+// float pair h + l: Knuth's TwoSum (D. E. Knuth, TAOCP vol. 2, 4.2.2) puts
+// each addition's rounding error into l.  In float64 these sums ran on the
+// float64 pipe (1/64 of the float32 rate): the n=18 mixed workload's finish
+// (1000 x 512 outputs, 45 segments) took 0.19 ms, twice its GEMM.
+__device__ __forceinline__ float seg_sum(const float *__restrict__ C, int64_t nseg, int64_t seg_stride, int64_t idx,
+                                         float start)
 {
-    double s = 0.0;
-    for (int64_t z = 0; z < nseg; ++z)
-        s += (double)C[z * seg_stride + idx];
-    return s;
+    float h = start, l = 0.f;
+    const float *c = C + idx;
+    for (int64_t z = 0; z < nseg; ++z, c += seg_stride)
+    {
+        const float x = *c;
+        const float s = __fadd_rn(h, x);
+        const float bb = __fsub_rn(s, h);
+        l = __fadd_rn(l, __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(x, bb)));
+        h = s;
+    }
+    return __fadd_rn(h, l);
 }
 
 // expectation: out[k][t] += (C[k][t], C[K+k][t])   (complex64 out)
@@ -372,8 +386,8 @@ __global__ void k_finish_expect(const float *__restrict__ C, int64_t nseg, int64
     {
         const int64_t k = e / S, t = e - k * S;
         float2 o = out[e];
-        o.x = (float)((double)o.x + seg_sum(C, nseg, seg_stride, k * cols_pad + t));
-        o.y = (float)((double)o.y + seg_sum(C, nseg, seg_stride, (K + k) * cols_pad + t));
+        o.x = seg_sum(C, nseg, seg_stride, k * cols_pad + t, o.x);
+        o.y = seg_sum(C, nseg, seg_stride, (K + k) * cols_pad + t, o.y);
         out[e] = o;
     }
 }
@@ -386,8 +400,8 @@ __global__ void k_finish_weighted(const float *__restrict__ C, int64_t nseg, int
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
     {
         const int64_t p = e / S, t = e - p * S;
-        W[e] = make_float2((float)seg_sum(C, nseg, seg_stride, p * cols_pad + t),
-                           (float)seg_sum(C, nseg, seg_stride, (P + p) * cols_pad + t));
+        W[e] = make_float2(seg_sum(C, nseg, seg_stride, p * cols_pad + t, 0.f),
+                           seg_sum(C, nseg, seg_stride, (P + p) * cols_pad + t, 0.f));
     }
 }
 
