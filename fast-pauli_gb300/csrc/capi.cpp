@@ -558,9 +558,14 @@ ExpectPlan plan_expect(const fpg_operator *op, int64_t S, bool fp32, const void 
     // per row lane.  The double-float kernels are issue-bound and gain from
     // fewer, longer CTAs (less epilogue and reduction per row); the float32
     // ones are bound by load latency and gain from more CTAs to pick from
+    // (float32 marginal kernel, mixed n=18 step: 6.92 / 6.84 / 6.93 / 7.08 ms
+    // at 6 / 12 / 24 / 48 CTAs per SM; transform kernel: 7.04 / 6.98 / 6.93 /
+    // 6.95 ms at 8 / 12 / 24 / 48)
     constexpr int kSplitCtasPerSmF64 = 4, kSplitCtasPerSmF32 = 24;
-    const int per_sm = fp32 ? kSplitCtasPerSmF32 : kSplitCtasPerSmF64;
-    auto pick = [per_sm](int64_t ctas_per_split, int64_t blocks, int row_lanes, bool windowed, int64_t window) {
+    constexpr int kSplitCtasPerSmF32Marg = 12, kSplitCtasPerSmF32Wht = 24;
+    const int per_sm_all = fp32 ? kSplitCtasPerSmF32 : kSplitCtasPerSmF64;
+    auto pick_at = [](int per_sm, int64_t ctas_per_split, int64_t blocks, int row_lanes, bool windowed,
+                      int64_t window) {
         if (ctas_per_split <= 0)
             return 1;
         const int64_t target = (int64_t)sm_count() * per_sm;
@@ -570,13 +575,18 @@ ExpectPlan plan_expect(const fpg_operator *op, int64_t S, bool fp32, const void 
         const int64_t mx = std::max<int64_t>(1, blocks / ((int64_t)row_lanes * 4));
         return (int)std::max<int64_t>(1, std::min<int64_t>(std::min(s, mx), 65535));
     };
+    auto pick = [&](int64_t ctas_per_split, int64_t blocks, int row_lanes, bool windowed, int64_t window) {
+        return pick_at(per_sm_all, ctas_per_split, blocks, row_lanes, windowed, window);
+    };
     p.fam_splits[kFamDirect] =
         pick((int64_t)op->fast_chunks.size() * p.n_ctiles, NB / 2, 256 / p.TC, over, kWindowBlocks);
     p.fam_splits[kFamPair] = pick((int64_t)op->pairs.size() * p.n_ctiles, NB / 2, 256 / p.TC, over, kWindowBlocks);
-    p.fam_splits[kFamMarg] =
-        pick((int64_t)op->margs.size() * p.wht_ctiles, NB / 2, 256 / p.wht_TC, over1, kWindowBlocks);
-    p.fam_splits[kFamWht] =
-        pick((int64_t)op->wht.size() * p.wht_ctiles, NB16 / 2, kWhtThreads / p.wht_TC, over1, 2 * kWindowBlocks);
+    p.fam_splits[kFamMarg] = pick_at(fp32 ? kSplitCtasPerSmF32Marg : kSplitCtasPerSmF64,
+                                     (int64_t)op->margs.size() * p.wht_ctiles, NB / 2, 256 / p.wht_TC, over1,
+                                     kWindowBlocks);
+    p.fam_splits[kFamWht] = pick_at(fp32 ? kSplitCtasPerSmF32Wht : kSplitCtasPerSmF64,
+                                    (int64_t)op->wht.size() * p.wht_ctiles, NB16 / 2, kWhtThreads / p.wht_TC, over1,
+                                    2 * kWindowBlocks);
     // the tile kernel: one element per lane (the V = 1 tiling), its column
     // tile within the L2 budget (its units read rows spread over the whole
     // state), the df64 copy of the state for the float64 path
