@@ -112,8 +112,8 @@ struct ArF32
     }
     // small elements: a block half's 32 loads are issued before any use
     static constexpr int kPrefetchRows = 16;
-    // row offsets from the CTA's table (the df64 form spilled with it and
-    // ran 1.04x slower; this form went 2.56 -> 1.92 ms per n=18 launch)
+    static constexpr int kBatchUnroll = 4;
+    // row offsets from the CTA's table: 2.56 -> 1.92 ms per n=18 launch
     static constexpr bool kRowTable = true;
     using raw_t = float2;
     static __device__ __forceinline__ raw_t ld(const in_t *psi, int64_t e)
@@ -140,6 +140,7 @@ struct ArF64
     using in_t = double;
     static constexpr bool kRaises = false, kRecompute = true;
     static constexpr int kPrefetchRows = 0;
+    static constexpr int kBatchUnroll = 4;
     static constexpr bool kRowTable = false;
     using raw_t = double2;
     static __device__ __forceinline__ raw_t ld(const in_t *, int64_t)
@@ -214,6 +215,7 @@ struct ArDF
     using in_t = double;
     static constexpr bool kRaises = true, kRecompute = false;
     static constexpr int kPrefetchRows = 0;
+    static constexpr int kBatchUnroll = 4;
     static constexpr bool kRowTable = false;
     using raw_t = float4;
     static __device__ __forceinline__ float4 raw_zero()
@@ -300,6 +302,12 @@ struct ArDFS : ArDF
     static constexpr bool kRaises = false, kRecompute = false;
     // 16-byte elements: loads issued four rows at a time ahead of use
     static constexpr int kPrefetchRows = 4;
+    // the batch loop rolled and the row offsets from the CTA's table: n=14
+    // weight<=2 step 2.185 -> 2.150 ms (rolled: the unrolled body missed the
+    // instruction cache) -> 2.072 ms (with the table, which spilled while the
+    // loop was unrolled)
+    static constexpr int kBatchUnroll = 1;
+    static constexpr bool kRowTable = true;
     static __device__ __forceinline__ void q(const in_t *psi, int64_t ea, int64_t eb, bool re, bool im, val &vr,
                                              val &vi, bool &)
     {
@@ -318,7 +326,7 @@ struct ArDFS : ArDF
 // Sums of one block: bt[part] (total) and bl[part][j] (rows whose visited-row
 // bit j is set).  LB = 5: all 32 rows, visited bit j = row bit j.  LB = 4:
 // the 16 rows with bit pl clear; visited bit j = row bit (j < pl ? j : j + 1).
-// TAB (the float32 policy, n >= 5, 32 S < 2^31): the element offsets of
+// TAB (policies with kRowTable, n >= 5, 32 S < 2^31): the element offsets of
 // the visited rows from the block's first row come from the CTA's table
 // s_rows ({row, partner row} x S, 32-bit), so a row load is one wide
 // multiply-add on a pointer formed once per block instead of 64-bit index
@@ -350,7 +358,9 @@ __device__ __forceinline__ void block_marginals(const typename A::in_t *__restri
         constexpr bool kElemPtr = std::is_same_v<typename A::in_t, typename A::raw_t>;
         [[maybe_unused]] const typename A::in_t *pa = psi + ((int64_t)base * S + t0);
         [[maybe_unused]] const typename A::in_t *pb = psi + ((int64_t)baseB * S + t0);
-#pragma unroll
+        // the half's four 4-row batches: unrolled, or (kBatchUnroll = 1) a
+        // loop, for a kernel body that stays in the instruction cache
+#pragma unroll(A::kBatchUnroll)
         for (int k = 0; k < 4; ++k)
         {
             if constexpr (A::kPrefetchRows > 0)
@@ -395,7 +405,10 @@ __device__ __forceinline__ void block_marginals(const typename A::in_t *__restri
                 v[u][1] = A::zero();
                 if constexpr (A::kPrefetchRows > 0)
                 {
-                    A::qraw(ra[(4 * k + u) % PF], rb[(4 * k + u) % PF], need_re, need_im, v[u][0], v[u][1]);
+                    // PF = 4: batch k's rows are ra[u] (a compile-time index
+                    // whether or not the batch loop is unrolled)
+                    const int ri = PF == 4 ? u : (4 * k + u) % PF;
+                    A::qraw(ra[ri], rb[ri], need_re, need_im, v[u][0], v[u][1]);
                 }
                 else
                 {
