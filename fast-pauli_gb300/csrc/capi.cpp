@@ -719,9 +719,12 @@ size_t apply_scratch_bytes(int n, int64_t S, int64_t n_cw, bool fp32)
     const int64_t n_elem = ((int64_t)1 << n) * S;
     if (fp32 || n_elem * 16 > kDfSplitMaxBytes)
         return 0;
-    return 256 + (size_t)n_elem * 16 + (size_t)n_cw * 16;
+    // flag, the column maxima of the states and of the coefficients, the
+    // df64 copies
+    return 256 + 2 * df_split_colmax_bytes(S) + (size_t)n_elem * 16 + (size_t)n_cw * 16;
 }
 
+// cw: n_cw = P coefficients (one column) or, weighted, (P, S) per column
 int run_apply(bool fp32, bool weighted, const DevOp &dop, const void *cw, int64_t n_cw, const void *states, void *out,
               int64_t S, cudaStream_t st)
 {
@@ -734,11 +737,14 @@ int run_apply(bool fp32, bool weighted, const DevOp &dop, const void *cw, int64_
     Scratch sc(st);
     FPG_CUDA(sc.alloc(bytes));
     int *flag = (int *)sc.p;
-    void *psi_df = (char *)sc.p + 256;
+    void *cm_psi = (char *)sc.p + 256;
+    void *cm_cw = (char *)cm_psi + df_split_colmax_bytes(S);
+    void *psi_df = (char *)cm_cw + df_split_colmax_bytes(S);
     void *cw_df = (char *)psi_df + (((int64_t)1 << dop.n) * S) * 16;
+    const int64_t cw_cols = (weighted && S > 0 && n_cw % S == 0) ? S : 1;
     FPG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
-    FPG_CUDA(launch_df_split(states, ((int64_t)1 << dop.n) * S, psi_df, flag, st));
-    FPG_CUDA(launch_df_split(cw, n_cw, cw_df, flag, st));
+    FPG_CUDA(launch_df_split(states, (int64_t)1 << dop.n, S, psi_df, cm_psi, flag, st));
+    FPG_CUDA(launch_df_split(cw, n_cw / cw_cols, cw_cols, cw_df, cm_cw, flag, st));
     FPG_CUDA(launch_apply_df(weighted, dop, cw_df, psi_df, out, S, flag, st));
     FPG_CUDA(launch_apply(false, weighted, dop, cw, states, out, S, st, flag));
     return FPG_OK;
@@ -755,7 +761,8 @@ int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int6
     // families' partial tables
     const bool need_flag =
         !fp32 && (!op->pairs.empty() || !op->tiles.empty() || !op->margs.empty() || !op->wht.empty());
-    const size_t flag_bytes = need_flag ? 256 : 0;
+    // (the flag, then the column maxima of the df64 range check)
+    const size_t flag_bytes = need_flag ? 256 + df_split_colmax_bytes(S) : 0;
     Scratch partial(st);
     if (scratch > 0 || need_flag)
         FPG_CUDA(partial.alloc(flag_bytes + (size_t)scratch * sizeof(double)));
@@ -763,13 +770,17 @@ int run_expect_strings(const fpg_operator *op, const void *psi, double *ev, int6
     if (need_flag)
         FPG_CUDA(cudaMemsetAsync(range_flag, 0, sizeof(int), st));
     double *partials = (double *)((char *)partial.p + flag_bytes);
-    // float64 path: the state split into df64 once (same size), when it fits
+    // float64 path: the state split into df64 once (same size), when it fits;
+    // otherwise the kernels split it themselves and the pass only checks the
+    // columns' range
     Scratch split(st);
     const int64_t n_elem = ((int64_t)1 << op->n) * S;
-    if (need_flag && n_elem * 16 <= kDfSplitMaxBytes)
+    if (need_flag)
     {
-        FPG_CUDA(split.alloc((size_t)n_elem * 16));
-        FPG_CUDA(launch_df_split(psi, n_elem, split.p, range_flag, st));
+        void *colmax = (char *)partial.p + 256;
+        if (n_elem * 16 <= kDfSplitMaxBytes)
+            FPG_CUDA(split.alloc((size_t)n_elem * 16));
+        FPG_CUDA(launch_df_split(psi, (int64_t)1 << op->n, S, split.p, colmax, range_flag, st));
     }
     const void *psi_df = split.p;
     // family f writes ev directly (caller order) or its own partial table
@@ -870,7 +881,8 @@ size_t request_scratch_bytes(const fpg_operator *op, int64_t K, int64_t S, bool 
     }
     const ExpectPlan plan = plan_expect(op, S, fp32, nullptr);
     int64_t off[kNumFam];
-    size_t b = P * (size_t)S * sizeof(double) + (size_t)family_partials(op, plan, S, off) * sizeof(double) + 512;
+    size_t b = P * (size_t)S * sizeof(double) + (size_t)family_partials(op, plan, S, off) * sizeof(double) + 512 +
+               df_split_colmax_bytes(S);
     const int64_t split_bytes = ((int64_t)1 << op->n) * S * 16;
     if (!fp32 && (!op->pairs.empty() || !op->tiles.empty() || !op->margs.empty() || !op->wht.empty()) &&
         split_bytes <= kDfSplitMaxBytes)

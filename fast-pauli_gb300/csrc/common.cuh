@@ -234,9 +234,13 @@ cudaError_t launch_expect_marg(bool fp32, const void *psi, int64_t S, int n, con
                                const MargChunk *d_chunks, int n_chunks, int max_high_bits, int TC, int n_ctiles,
                                int n_splits, double *out, int *range_flag, const void *psi_df, cudaStream_t st);
 
-// out[i] = complex128 psi[i] as df64 (re_h, re_l, im_h, im_l) floats, i <
-// count; raises *range_flag for values outside the df64 range.
-cudaError_t launch_df_split(const void *psi, int64_t count, void *out, int *range_flag, cudaStream_t st);
+// out[i] = complex128 psi[i] as df64 (re_h, re_l, im_h, im_l) floats for the
+// rows x cols row-major elements (out null: the range check only); raises
+// *range_flag for elements or columns outside the df64 range (df64.cuh).
+// colmax: df_split_colmax_bytes(cols) of scratch.
+cudaError_t launch_df_split(const void *psi, int64_t rows, int64_t cols, void *out, void *colmax, int *range_flag,
+                            cudaStream_t st);
+size_t df_split_colmax_bytes(int64_t cols);
 // State size up to which the float64 path splits the state into a scratch
 // copy once per call instead of inside every kernel.
 constexpr int64_t kDfSplitMaxBytes = int64_t(16) << 30;

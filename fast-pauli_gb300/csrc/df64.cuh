@@ -42,17 +42,25 @@ __device__ __forceinline__ void split_bits(uint32_t bl, uint32_t bh, float &hi, 
     lo = __uint_as_float(__float_as_uint(l) | sign);
 }
 
-// Range of the df64 kernels: float64 inputs with 2^-90 <= |x| < 2^40 (or
-// zero / subnormal, taken as zero) keep every product, error term and sum of
-// up to 2^40 terms inside float's normal range.  A kernel that meets a value
-// outside it raises a per-call flag, and the float64 form of the kernel,
-// launched after it on the same stream, then recomputes the result (it
-// returns at once while the flag is clear).  bh = high word of the float64.
+// Range of the df64 kernels.  Per element: |x| < 2^40, so that products
+// (< 2^80) and sums of up to 2^40 of them stay below float's largest value.
+// Per state column (and over an operand such as the coefficients): the
+// largest |x| at least 2^-39 unless the column is all zero, so that the
+// products that make up its results (down to 2^-78) and their error terms
+// (2^-48 smaller) stay in float's normal range; values far below a column's
+// largest contribute errors below 2^-126 each, far below 2^-48 of its
+// results.  A kernel that meets an element outside the first bound, or the
+// split pass (k_df_split) a column outside the second, raises a per-call
+// flag, and the float64 form of the kernel, launched after it on the same
+// stream, then recomputes the result (it returns at once while the flag is
+// clear).  bh = high word of the float64.
 __device__ __forceinline__ bool df_out_of_range(uint32_t bh)
 {
-    const uint32_t E = (bh >> 20) & 0x7ffu;
-    return E != 0u && (E - (1023u - 90u)) >= 130u; // E outside [933, 1062]
+    return ((bh >> 20) & 0x7ffu) >= 1023u + 40u; // |x| >= 2^40, inf or nan
 }
+
+// The column bound as the high word of |x| (monotone in |x|): 2^-39
+constexpr uint32_t kDfColumnMinKey = (1023u - 39u) << 20;
 
 // One complex128 amplitude as df64: (re_h, re_l, im_h, im_l) from its four
 // 32-bit words; bad |= a part outside the df64 range.

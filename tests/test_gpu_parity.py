@@ -374,12 +374,15 @@ def test_marginal_kernel_groups_per_string(n, S):
     op.close()
 
 
-@pytest.mark.parametrize("scale_psi,scale_h", [(1.0, 1.0), (1e-30, 1.0), (1e15, 1.0), (1.0, 1e20), (1.0, 1e-35)])
+@pytest.mark.parametrize("scale_psi,scale_h", [(1.0, 1.0), (1e-30, 1.0), (1e-20, 1.0), (1e-12, 1.0), (1e15, 1.0),
+                                               (1.0, 1e20), (1.0, 1e-35)])
 def test_float64_path_far_from_unit_scale(scale_psi, scale_h):
     """The float64 path runs its kernels in double-float arithmetic on the
-    float32 pipes for values within 2^-90 .. 2^40 and recomputes in float64
-    otherwise: results must meet the float64 tolerance at any scale, and for
-    states with exact zeros (basis states)."""
+    float32 pipes for elements below 2^40 in states whose columns reach 2^-39,
+    and recomputes in float64 otherwise: results must meet the float64
+    tolerance at any scale (1e-20: every element above the old per-element
+    bound of 2^-90, products below float's normal range), and for states
+    with exact zeros (basis states)."""
     rng = np.random.default_rng(61)
     n, S, K = 9, 12, 5
     strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
@@ -394,7 +397,8 @@ def test_float64_path_far_from_unit_scale(scale_psi, scale_h):
     assert normwise(got, want) < TOL_C128
 
 
-@pytest.mark.parametrize("scale_psi,scale_h", [(1.0, 1.0), (1e-30, 1.0), (1e15, 1.0), (1.0, 1e20), (1.0, 1e-35)])
+@pytest.mark.parametrize("scale_psi,scale_h", [(1.0, 1.0), (1e-30, 1.0), (1e15, 1.0), (1.0, 1e20), (1.0, 1e-35),
+                                               (1e-20, 1e-20), (1e-20, 1.0)])
 def test_float64_apply_far_from_unit_scale(scale_psi, scale_h):
     """The float64 apply runs in double-float arithmetic on the float32 pipes
     when states and coefficients lie within 2^-90 .. 2^40 and in float64
@@ -832,3 +836,43 @@ def test_family_stats_partition_the_operator_work():
     assert fam["marginal"][0] == 14 * half
     assert fam["transform"][0] == 1 << n
     assert fam["pair"] == (0, 0) and fam["direct"] == (0, 0)
+
+
+@pytest.mark.parametrize("tiny", [2.0**-70, 2.0**-45, 1e-35])
+def test_float64_columns_of_very_different_scale(tiny):
+    """Each state column is its own state: a column scaled far below the
+    others (uniform amplitudes of 2^-70 or 2^-45, above the old per-element
+    bound of 2^-90, or a Gaussian column at 1e-35) keeps float64 accuracy
+    relative to its own values (such a column sends the call to the float64
+    recomputation)."""
+    rng = np.random.default_rng(71)
+    n, S, K = 10, 6, 4
+    strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
+    P = len(strings)
+    h = rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    psi[:, 1] = tiny * (1 + 1j)  # uniform tiny column
+    psi[:, 2] *= tiny            # Gaussian tiny column
+    want = oracle.summed_expectation(strings, h, psi)
+    got = fp.SummedPauliOp(strings, h).expectation_value(psi)
+    for t in range(S):
+        assert normwise(got[:, t], want[:, t]) < TOL_C128, t
+
+
+def test_float64_noise_amplitudes_stay_on_the_double_float_path():
+    """Amplitudes of 1e-40 (below 2^-90) beside unit-scale ones: the column's
+    largest value sets the df64 range, the tiny ones contribute errors below
+    2^-126 each, and the results keep float64 accuracy per column."""
+    rng = np.random.default_rng(72)
+    n, S = 10, 5
+    strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
+    P = len(strings)
+    h = rng.standard_normal((P, 3)) + 1j * rng.standard_normal((P, 3))
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    for t in range(S):
+        psi[rng.choice(1 << n, 64, replace=False), t] = 1e-40 * (1 - 1j)
+    for coeffs in (h, np.eye(P, dtype=np.complex128)):
+        want = oracle.summed_expectation(strings, coeffs, psi)
+        got = fp.SummedPauliOp(strings, coeffs).expectation_value(psi)
+        for t in range(S):
+            assert normwise(got[:, t], want[:, t]) < TOL_C128, t
