@@ -401,8 +401,9 @@ def test_float64_path_far_from_unit_scale(scale_psi, scale_h):
                                                (1e-20, 1e-20), (1e-20, 1.0)])
 def test_float64_apply_far_from_unit_scale(scale_psi, scale_h):
     """The float64 apply runs in double-float arithmetic on the float32 pipes
-    when states and coefficients lie within 2^-90 .. 2^40 and in float64
-    otherwise (the double-float kernel then leaves the output untouched)."""
+    when the elements of states and coefficients stay below 2^40 and their
+    columns reach 2^-39, and in float64 otherwise (the double-float kernel
+    then leaves the output untouched)."""
     rng = np.random.default_rng(64)
     n, S, K = 8, 40, 3
     strings = oracle.uniform_strings(rng, n, 50) + oracle.calculate_pauli_strings_max_weight(n, 1)[1:]
