@@ -380,8 +380,8 @@ def test_float64_path_far_from_unit_scale(scale_psi, scale_h):
     """The float64 path runs its kernels in double-float arithmetic on the
     float32 pipes for elements below 2^40 in states whose columns reach 2^-39,
     and recomputes in float64 otherwise: results must meet the float64
-    tolerance at any scale (1e-20: every element above the old per-element
-    bound of 2^-90, products below float's normal range), and for states
+    tolerance at any scale (1e-20: every element above 2^-90, yet products
+    below float's normal range), and for states
     with exact zeros (basis states)."""
     rng = np.random.default_rng(61)
     n, S, K = 9, 12, 5
@@ -842,8 +842,8 @@ def test_family_stats_partition_the_operator_work():
 @pytest.mark.parametrize("tiny", [2.0**-70, 2.0**-45, 1e-35])
 def test_float64_columns_of_very_different_scale(tiny):
     """Each state column is its own state: a column scaled far below the
-    others (uniform amplitudes of 2^-70 or 2^-45, above the old per-element
-    bound of 2^-90, or a Gaussian column at 1e-35) keeps float64 accuracy
+    others (uniform amplitudes of 2^-70 or 2^-45, whose products fall below
+    float's normal range, or a Gaussian column at 1e-35) keeps float64 accuracy
     relative to its own values (such a column sends the call to the float64
     recomputation)."""
     rng = np.random.default_rng(71)
