@@ -331,13 +331,16 @@ struct ArDFS : ArDF
 // s_rows ({row, partner row} x S, 32-bit), so a row load is one wide
 // multiply-add on a pointer formed once per block instead of 64-bit index
 // arithmetic per row.
-template <typename A, int LB, bool TAB>
+// BOTHP: the chunk needs both parts (need_re and need_im), known at compile
+// time so that no q or tree step is conditional.
+template <typename A, int LB, bool TAB, bool BOTHP>
 __device__ __forceinline__ void block_marginals(const typename A::in_t *__restrict__ psi, int64_t S, int64_t t0,
                                                 uint64_t base, uint64_t baseB, uint32_t xl, int pl, int RB,
-                                                bool need_re, bool need_im, typename A::val (&bt)[2],
+                                                bool need_re_, bool need_im_, typename A::val (&bt)[2],
                                                 typename A::val (&bl)[2][5], bool &bad, const int2 *s_rows)
 {
     using val = typename A::val;
+    const bool need_re = BOTHP || need_re_, need_im = BOTHP || need_im_;
     [[maybe_unused]] const typename A::raw_t *qa = nullptr, *qb = nullptr;
     if constexpr (TAB)
     {
@@ -568,12 +571,21 @@ __global__ void __launch_bounds__(256, 2)
 #pragma unroll
                 for (int j = 0; j < 5; ++j)
                     bl[p][j] = A::zero();
-            if (pl < 0)
-                block_marginals<A, 5, TAB>(psi, S, t0, base, baseB, xl, pl, RB, need_re, need_im, bt, bl, bad,
-                                           s_rows);
+            if (need_re && need_im)
+            {
+                if (pl < 0)
+                    block_marginals<A, 5, TAB, true>(psi, S, t0, base, baseB, xl, pl, RB, true, true, bt, bl, bad,
+                                                     s_rows);
+                else
+                    block_marginals<A, 4, TAB, true>(psi, S, t0, base, baseB, xl, pl, RB, true, true, bt, bl, bad,
+                                                     s_rows);
+            }
+            else if (pl < 0)
+                block_marginals<A, 5, TAB, false>(psi, S, t0, base, baseB, xl, pl, RB, need_re, need_im, bt, bl, bad,
+                                                  s_rows);
             else
-                block_marginals<A, 4, TAB>(psi, S, t0, base, baseB, xl, pl, RB, need_re, need_im, bt, bl, bad,
-                                           s_rows);
+                block_marginals<A, 4, TAB, false>(psi, S, t0, base, baseB, xl, pl, RB, need_re, need_im, bt, bl, bad,
+                                                  s_rows);
             const uint64_t hi = base & hi_mask;
             if (in_run && hi != run_hi)
             {
