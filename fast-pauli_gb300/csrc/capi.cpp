@@ -233,13 +233,18 @@ void free_dev(fpg_operator *op)
 
 // The tile family: pair-kernel groups x = 2^a + 2^b (a < b) whose z' lie in
 // {0, 2^a}, gathered into units of four row bits Q with up to six groups
-// whose both bits lie in Q (k_expect_tile.cu).  Greedy cover: the first
-// group left opens a unit; its other two bits are the ones that bring the
-// most groups left into it.  Taken groups leave op->pairs for op->tiles /
+// whose both bits lie in Q (k_expect_tile.cu).  Greedy cover: up to
+// kTileMaxCoverQubits qubits each unit is the set of four bits that covers
+// the most groups left (all 153 pairs of 18 qubits: 29 units; the lower
+// bound is 27); above it the first group left opens a unit and its other two
+// bits are the ones that bring the most groups left into it (32 units for
+// the same pairs; 18 for the 91 pairs of 14 qubits either way, which is
+// optimal).  Taken groups leave op->pairs for op->tiles /
 // op->tile_pairs and is_wht 4.  Operators on fewer than kTileMinQubits
 // qubits, or with fewer than kTileMinGroups such groups, keep the pair kernel.
 constexpr int kTileMinQubits = 8;
 constexpr int kTileMinGroups = 6;
+constexpr int kTileMaxCoverQubits = 24; // C(24, 4) = 10626 candidate sets per unit
 
 void build_tiles(fpg_operator *op, const std::vector<size_t> &pair_groups, std::vector<char> &is_wht)
 {
@@ -270,33 +275,67 @@ void build_tiles(fpg_operator *op, const std::vector<size_t> &pair_groups, std::
     size_t scan = 0;
     while (left > 0)
     {
-        while (at[scan] < 0)
-            ++scan;
-        const int a = (int)(scan / (size_t)n), b = (int)(scan % (size_t)n);
-        int best = -1, bc = -1, bd = -1;
-        for (int c = 0; c < n; ++c)
+        int q[4];
+        if (n <= kTileMaxCoverQubits)
         {
-            if (c == a || c == b)
-                continue;
-            for (int d = c + 1; d < n; ++d)
-            {
-                if (d == a || d == b)
-                    continue;
-                const int q[4] = {a, b, c, d};
-                int cnt = 0;
-                for (int i = 0; i < 4; ++i)
-                    for (int j = i + 1; j < 4; ++j)
-                        cnt += cell(q[i], q[j]) >= 0;
-                if (cnt > best)
+            // the set of four row bits that covers the most groups left (the
+            // first such set in lexicographic order)
+            int best = -1;
+            for (int a = 0; a < n; ++a)
+                for (int b = a + 1; b < n; ++b)
                 {
-                    best = cnt;
-                    bc = c;
-                    bd = d;
+                    const int ab = cell(a, b) >= 0;
+                    for (int c = b + 1; c < n; ++c)
+                    {
+                        const int abc = ab + (cell(a, c) >= 0) + (cell(b, c) >= 0);
+                        for (int d = c + 1; d < n; ++d)
+                        {
+                            const int cnt = abc + (cell(a, d) >= 0) + (cell(b, d) >= 0) + (cell(c, d) >= 0);
+                            if (cnt > best)
+                            {
+                                best = cnt;
+                                q[0] = a;
+                                q[1] = b;
+                                q[2] = c;
+                                q[3] = d;
+                            }
+                        }
+                    }
+                }
+        }
+        else
+        {
+            while (at[scan] < 0)
+                ++scan;
+            const int a = (int)(scan / (size_t)n), b = (int)(scan % (size_t)n);
+            int best = -1, bc = -1, bd = -1;
+            for (int c = 0; c < n; ++c)
+            {
+                if (c == a || c == b)
+                    continue;
+                for (int d = c + 1; d < n; ++d)
+                {
+                    if (d == a || d == b)
+                        continue;
+                    const int qq[4] = {a, b, c, d};
+                    int cnt = 0;
+                    for (int i = 0; i < 4; ++i)
+                        for (int j = i + 1; j < 4; ++j)
+                            cnt += cell(qq[i], qq[j]) >= 0;
+                    if (cnt > best)
+                    {
+                        best = cnt;
+                        bc = c;
+                        bd = d;
+                    }
                 }
             }
+            q[0] = a;
+            q[1] = b;
+            q[2] = bc;
+            q[3] = bd;
+            std::sort(q, q + 4);
         }
-        int q[4] = {a, b, bc, bd};
-        std::sort(q, q + 4);
         TileChunk t{};
         for (int k = 0; k < 4; ++k)
             t.q[k] = (int8_t)q[k];
