@@ -877,3 +877,31 @@ def test_float64_noise_amplitudes_stay_on_the_double_float_path():
         got = fp.SummedPauliOp(strings, coeffs).expectation_value(psi)
         for t in range(S):
             assert normwise(got[:, t], want[:, t]) < TOL_C128, t
+
+
+@pytest.mark.parametrize("n,S", [(8, 6), (10, 40), (12, 33), (14, 64), (9, 1)])
+def test_float64_tile_kernel_all_pairs(n, S):
+    """The float64 two-position groups (XX, XY, YX, YY on every pair of
+    qubits: the tile kernel's units cover them all): per-string values to
+    1e-13 and the summed expectation values to the float64 tolerance against
+    the oracle, for even and odd state counts."""
+    torch = pytest.importorskip("torch")
+    from fast_pauli import _abi
+
+    rng = np.random.default_rng(900 + 10 * n + S)
+    strings = [s for s in oracle.calculate_pauli_strings(n, 2) if sum(c in "XY" for c in s) == 2]
+    P, K = len(strings), 3
+    psi = oracle.unit_norm_states(rng, 1 << n, S)
+    L = _abi.lib()
+    op = _abi.Operator(strings)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    dpsi = torch.from_numpy(psi).cuda()
+    ev = torch.empty((P, S), dtype=torch.float64, device="cuda")
+    _abi.check(L.fpg_expect_strings(op.handle, dpsi.data_ptr(), ev.data_ptr(), S, _abi.FPG_C128, st))
+    torch.cuda.synchronize()
+    op.close()
+    want = np.stack([oracle.string_expectation(s, psi).real for s in strings])
+    assert np.abs(ev.cpu().numpy() - want).max() < 1e-13
+    h = rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))
+    got = fp.SummedPauliOp(strings, h).expectation_value(dpsi).cpu().numpy()
+    assert normwise(got, oracle.summed_expectation(strings, h, psi)) < TOL_C128
