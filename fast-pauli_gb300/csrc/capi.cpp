@@ -602,6 +602,10 @@ ExpectPlan plan_expect(const fpg_operator *op, int64_t S, bool fp32, const void 
     // 6.95 ms at 8 / 12 / 24 / 48)
     constexpr int kSplitCtasPerSmF64 = 4, kSplitCtasPerSmF32 = 24;
     constexpr int kSplitCtasPerSmF32Marg = 12, kSplitCtasPerSmF32Wht = 24;
+    // (float64, n=14 weight<=2 step: marginal kernel 2.156 / 2.044 / 2.108 /
+    // 2.128 ms at 2 / 4 / 8 / 16 CTAs per SM; transform kernel 2.100 / 2.044 /
+    // 2.048 ms at 2 / 4 / 8)
+    constexpr int kSplitCtasPerSmF64Marg = 4, kSplitCtasPerSmF64Wht = 4;
     const int per_sm_all = fp32 ? kSplitCtasPerSmF32 : kSplitCtasPerSmF64;
     auto pick_at = [](int per_sm, int64_t ctas_per_split, int64_t blocks, int row_lanes, bool windowed,
                       int64_t window) {
@@ -620,10 +624,10 @@ ExpectPlan plan_expect(const fpg_operator *op, int64_t S, bool fp32, const void 
     p.fam_splits[kFamDirect] =
         pick((int64_t)op->fast_chunks.size() * p.n_ctiles, NB / 2, 256 / p.TC, over, kWindowBlocks);
     p.fam_splits[kFamPair] = pick((int64_t)op->pairs.size() * p.n_ctiles, NB / 2, 256 / p.TC, over, kWindowBlocks);
-    p.fam_splits[kFamMarg] = pick_at(fp32 ? kSplitCtasPerSmF32Marg : kSplitCtasPerSmF64,
+    p.fam_splits[kFamMarg] = pick_at(fp32 ? kSplitCtasPerSmF32Marg : kSplitCtasPerSmF64Marg,
                                      (int64_t)op->margs.size() * p.wht_ctiles, NB / 2, 256 / p.wht_TC, over1,
                                      kWindowBlocks);
-    p.fam_splits[kFamWht] = pick_at(fp32 ? kSplitCtasPerSmF32Wht : kSplitCtasPerSmF64,
+    p.fam_splits[kFamWht] = pick_at(fp32 ? kSplitCtasPerSmF32Wht : kSplitCtasPerSmF64Wht,
                                     (int64_t)op->wht.size() * p.wht_ctiles, NB16 / 2, kWhtThreads / p.wht_TC, over1,
                                     2 * kWindowBlocks);
     // the tile kernel: one element per lane (the V = 1 tiling), its column
