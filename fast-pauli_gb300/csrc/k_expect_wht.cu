@@ -52,6 +52,9 @@ struct W32
         float v, c;
     };
     static constexpr bool kRecompute = false;
+    // the two-level transform also with 16 row lanes (its 16-point second
+    // level spills the df64 and float64 forms)
+    static constexpr bool kTwoLevel16 = true;
     static __device__ __forceinline__ val zero()
     {
         return 0.f;
@@ -111,6 +114,9 @@ struct W64
     using cell = double;
     using acc = double;
     static constexpr bool kRecompute = true;
+    // the two-level transform also with 16 row lanes (its 16-point second
+    // level spills the df64 and float64 forms)
+    static constexpr bool kTwoLevel16 = false;
     static __device__ __forceinline__ val zero()
     {
         return 0.0;
@@ -167,6 +173,9 @@ struct WDF
     using cell = float2;
     using acc = DFv;
     static constexpr bool kRecompute = false;
+    // the two-level transform also with 16 row lanes (its 16-point second
+    // level spills the df64 and float64 forms)
+    static constexpr bool kTwoLevel16 = false;
     static __device__ __forceinline__ val zero()
     {
         return DFv{0.f, 0.f};
@@ -393,13 +402,16 @@ __global__ void __launch_bounds__(kWhtThreads, BOTH ? 1 : 2)
     const int64_t b1 = min(nblk, b0 + per);
     const int G = ch.count;
     const bool need_re = ch.n_even > 0, need_im = ch.n_even < G;
-    // two levels: x below the block (x < 16) and 8 row lanes -- the round's 8
-    // blocks differ only in block-index bits 0..2 (row bits 4..6), so a
-    // string's sign over them factors as (-1)^popc(base_0 & z) times the
-    // 8-point Walsh-Hadamard kernel at (z >> 4) & 7: one more 8-point
-    // transform per (coefficient, column) and a round costs each string one
-    // read instead of eight signed adds
-    const bool two_level = !paired && TR == 8;
+    // two levels: x below the block (x < 16) and TR = 8 row lanes (or 16, in
+    // the float32 form) --
+    // the round's TR blocks differ only in block-index bits below log2 TR
+    // (row bits 4..), so a string's sign over them factors as
+    // (-1)^popc(base_0 & z) times the TR-point Walsh-Hadamard kernel at
+    // (z >> 4) & (TR - 1): one more TR-point transform per (coefficient,
+    // column) and a round costs each string one read instead of TR signed
+    // adds (16 row lanes: the float32 form at n = 18, whose column tile of 16
+    // lanes fits the L2 budget)
+    const bool two_level = !paired && (TR == 8 || (W::kTwoLevel16 && TR == 16));
 
     // chunk strings' z masks in shared memory; this thread owns k = tr + j * TR
     for (int k = tid; k < G; k += blockDim.x)
@@ -469,7 +481,15 @@ __global__ void __launch_bounds__(kWhtThreads, BOTH ? 1 : 2)
         if (two_level)
         {
             // the parts written above: both, or the one the chunk's strings read
-            wht_rounds<W, 8>(wsm, TR, TC, BOTH ? 0 : (need_re ? 0 : 1), BOTH ? 2 : 1);
+            if constexpr (W::kTwoLevel16)
+            {
+                if (TR == 16)
+                    wht_rounds<W, 16>(wsm, TR, TC, BOTH ? 0 : (need_re ? 0 : 1), BOTH ? 2 : 1);
+                else
+                    wht_rounds<W, 8>(wsm, TR, TC, BOTH ? 0 : (need_re ? 0 : 1), BOTH ? 2 : 1);
+            }
+            else
+                wht_rounds<W, 8>(wsm, TR, TC, BOTH ? 0 : (need_re ? 0 : 1), BOTH ? 2 : 1);
             __syncthreads();
             const uint64_t base0 = s_base[0];
 #pragma unroll
@@ -482,7 +502,8 @@ __global__ void __launch_bounds__(kWhtThreads, BOTH ? 1 : 2)
                 // with one transform (!BOTH) its cells sit in the part the
                 // chunk's strings read
                 const int part = BOTH ? (k >= ch.n_even ? 1 : 0) : (need_re ? 0 : 1);
-                const cell c = wsm[(size_t)(((part * TR + (int)((z >> 4) & 7u)) * 16) + (int)(z & 15u)) * TC + tc];
+                const cell c =
+                    wsm[(size_t)(((part * TR + (int)((z >> 4) & (uint64_t)(TR - 1))) * 16) + (int)(z & 15u)) * TC + tc];
                 val sum = W::zero();
                 W::add_cell(sum, c, (__popcll(base0 & z) & 1) != 0);
                 W::acc_add(sums[j], sum);

@@ -792,15 +792,17 @@ def _strings_on_bits(n, xbit, zpairs, xchar="X"):
 
 
 @pytest.mark.parametrize("n,xbit", [(6, 1), (6, 5), (10, 1), (10, 3), (10, 6)])
-@pytest.mark.parametrize("S", [5, 40])
+@pytest.mark.parametrize("S", [5, 12, 40])
 @pytest.mark.parametrize("c64", [False, True])
 def test_transform_kernel_groups_with_two_bit_signs(n, xbit, S, c64):
     """Groups of >= 10 strings sharing one x whose signs use two row bits go
     to the transform kernel.  x below the 16-row block (x = 2, 8) with 40
     states (32 column lanes, 8 row lanes) takes the second level across a
-    round's 8 blocks -- at n = 6 the round holds fewer blocks than that; x =
-    32, 64 pairs blocks and keeps per-block sums; 5 states (8 column lanes,
-    32 row lanes) keep one level.  X and Y on the same bit give both parts."""
+    round's 8 blocks -- at n = 6 the round holds fewer blocks than that; with
+    12 states (16 column lanes, 16 row lanes) the float32 form takes a
+    16-point second level and the float64 forms keep one level; x = 32, 64
+    pairs blocks and keeps per-block sums; 5 states (8 column lanes, 32 row
+    lanes) keep one level.  X and Y on the same bit give both parts."""
     torch = pytest.importorskip("torch")
     K = 3
     rng = np.random.default_rng(50 + 7 * n + xbit + S)
