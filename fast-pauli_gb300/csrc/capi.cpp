@@ -767,18 +767,61 @@ size_t apply_scratch_bytes(int n, int64_t S, int64_t n_cw, bool fp32)
     return 256 + 2 * df_split_colmax_bytes(S) + (size_t)n_elem * 16 + (size_t)n_cw * 16;
 }
 
+// The group-diagonal table of a plain apply (launch_group_diag) in bytes, or
+// 0 where the kernels sum each group's strings in registers: apply_weighted
+// (its diagonals differ per column), fewer than 4 columns or fewer than two
+// strings per group on average (the table saves little), or a table above
+// kDiagTableMaxBytes.  The table (16 bytes per group and row in df64, 8 in
+// float32) replaces, per column, one signed sum over the group's strings.
+constexpr size_t kDiagTableMaxBytes = size_t(1) << 30;
+size_t diag_table_bytes(const DevOp &dop, int64_t S, bool weighted, bool fp32)
+{
+    if (weighted || S < 4 || dop.G <= 0 || dop.P < 2 * dop.G)
+        return 0;
+    const size_t b = ((size_t)dop.G << dop.n) * (fp32 ? 8 : 16);
+    return b <= kDiagTableMaxBytes ? b : 0;
+}
+
+// Scratch for `base` bytes and, when `tab` > 0, a table after them at a
+// 256-byte offset (returned in *diag).  Without room for the table, `tab` is
+// dropped (the kernels then sum in registers) rather than failing the call.
+cudaError_t alloc_with_table(Scratch &sc, size_t base, size_t tab, void **diag)
+{
+    *diag = nullptr;
+    const size_t off = (base + 255) & ~size_t(255);
+    if (tab)
+    {
+        if (sc.alloc(off + tab) == cudaSuccess)
+        {
+            *diag = (char *)sc.p + off;
+            return cudaSuccess;
+        }
+        cudaGetLastError();
+        sc.p = nullptr;
+    }
+    return base ? sc.alloc(base) : cudaSuccess;
+}
+
 // cw: n_cw = P coefficients (one column) or, weighted, (P, S) per column
 int run_apply(bool fp32, bool weighted, const DevOp &dop, const void *cw, int64_t n_cw, const void *states, void *out,
               int64_t S, cudaStream_t st)
 {
     const size_t bytes = apply_scratch_bytes(dop.n, S, n_cw, fp32);
+    Scratch sc(st);
+    void *diag = nullptr;
     if (bytes == 0)
     {
-        FPG_CUDA(launch_apply(fp32, weighted, dop, cw, states, out, S, st));
+        // float32 (or a float64 state too large for its df64 copy)
+        if (fp32)
+        {
+            FPG_CUDA(alloc_with_table(sc, 0, diag_table_bytes(dop, S, weighted, true), &diag));
+            if (diag)
+                FPG_CUDA(launch_group_diag(false, dop, cw, diag, nullptr, st));
+        }
+        FPG_CUDA(launch_apply(fp32, weighted, dop, cw, states, out, S, st, nullptr, diag));
         return FPG_OK;
     }
-    Scratch sc(st);
-    FPG_CUDA(sc.alloc(bytes));
+    FPG_CUDA(alloc_with_table(sc, bytes, diag_table_bytes(dop, S, weighted, false), &diag));
     int *flag = (int *)sc.p;
     void *cm_psi = (char *)sc.p + 256;
     void *cm_cw = (char *)cm_psi + df_split_colmax_bytes(S);
@@ -788,7 +831,9 @@ int run_apply(bool fp32, bool weighted, const DevOp &dop, const void *cw, int64_
     FPG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
     FPG_CUDA(launch_df_split(states, (int64_t)1 << dop.n, S, psi_df, cm_psi, flag, st));
     FPG_CUDA(launch_df_split(cw, n_cw / cw_cols, cw_cols, cw_df, cm_cw, flag, st));
-    FPG_CUDA(launch_apply_df(weighted, dop, cw_df, psi_df, out, S, flag, st));
+    if (diag)
+        FPG_CUDA(launch_group_diag(true, dop, cw_df, diag, flag, st));
+    FPG_CUDA(launch_apply_df(weighted, dop, cw_df, psi_df, out, S, flag, st, diag));
     FPG_CUDA(launch_apply(false, weighted, dop, cw, states, out, S, st, flag));
     return FPG_OK;
 }

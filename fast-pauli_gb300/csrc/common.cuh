@@ -302,13 +302,21 @@ cudaError_t launch_prep_coeffs(bool fp32, const DevOp &op, const void *coeffs, i
 
 // out(D,S) += sum_g psi[i^x_g] * sum_{j in g} cw[j] * (-1)^popc(i & z_j).
 // weighted: cw is (P_sorted, S) complex per column (already * phase, sorted order).
+// diag (float32, not weighted): the group diagonals from launch_group_diag.
 cudaError_t launch_apply(bool fp32, bool weighted, const DevOp &op, const void *cw, const void *psi, void *out,
-                         int64_t S, cudaStream_t st, const int *only_if = nullptr);
+                         int64_t S, cudaStream_t st, const int *only_if = nullptr, const void *diag = nullptr);
 // The float64 apply in df64: cw_df / psi_df are the df64 copies (float4 per
 // complex value, launch_df_split) of cw and psi; returns at once when
-// *skip_if is set (launch_apply with only_if = skip_if then runs).
+// *skip_if is set (launch_apply with only_if = skip_if then runs).  diag (not
+// weighted): the df64 group diagonals from launch_group_diag.
 cudaError_t launch_apply_df(bool weighted, const DevOp &op, const void *cw_df, const void *psi_df, void *out,
-                            int64_t S, const int *skip_if, cudaStream_t st);
+                            int64_t S, const int *skip_if, cudaStream_t st, const void *diag = nullptr);
+// The group diagonals of a plain apply, diag[g * 2^n + i] = (D_g)_ii for
+// every x-group g and row i, from the sorted-order coefficients cw (P values,
+// already times the phase): float2 per entry from float32 cw, or (df) float4
+// df64 per entry from cw's df64 copy.  Returns at once when skip_if is set.
+cudaError_t launch_group_diag(bool df, const DevOp &op, const void *cw, void *diag, const int *skip_if,
+                              cudaStream_t st);
 
 // W(P,S) in caller order -> sorted order with phase: cw[s,t] = W[orig[s],t] * (-i)^nY
 cudaError_t launch_prep_weighted(bool fp32, const DevOp &op, const void *W, int64_t S, void *cw_sorted,

@@ -97,14 +97,118 @@ __device__ __forceinline__ uint32_t sign_bits(const StringRec &rec, uint64_t i0)
     return (rec.mask_lo >> (uint32_t)(i0 & 31u)) ^ (0u - hi);
 }
 
+// (D_g)_ii of rows i0 .. i0+R-1 (one 32-row block) for column t: the group's
+// coefficients, signed per row, summed in sorted string order from zero.
+template <typename T, int R, bool WEIGHTED>
+__device__ __forceinline__ void group_diag(const Group &gr, const StringRec *__restrict__ recs,
+                                           const typename C2<T>::type *__restrict__ cw, int64_t S, int64_t t,
+                                           uint64_t i0, T (&wr)[R], T (&wi)[R])
+{
+    using CT = typename C2<T>::type;
+#pragma unroll
+    for (int k = 0; k < R; ++k)
+        wr[k] = wi[k] = T(0);
+    for (int32_t s = gr.begin; s < gr.begin + gr.count; ++s)
+    {
+        const uint32_t sb = sign_bits(recs[s], i0);
+        const CT c = WEIGHTED ? cw[(int64_t)s * S + t] : cw[s];
+#pragma unroll
+        for (int k = 0; k < R; ++k)
+        {
+            if ((sb >> k) & 1u)
+            {
+                wr[k] -= c.x;
+                wi[k] -= c.y;
+            }
+            else
+            {
+                wr[k] += c.x;
+                wi[k] += c.y;
+            }
+        }
+    }
+}
+
+// The same in df64 from the coefficients' df64 copies (float4 per complex
+// value): the first string's signed value, then a renormalised TwoSum per
+// string.
+template <int R, bool WEIGHTED>
+__device__ __forceinline__ void group_diag_df(const Group &gr, const StringRec *__restrict__ recs,
+                                              const float4 *__restrict__ cw, int64_t S, int64_t t, uint64_t i0,
+                                              float (&wr)[R][2], float (&wi)[R][2])
+{
+    {
+        const uint32_t sb = sign_bits(recs[gr.begin], i0);
+        const float4 c = WEIGHTED ? cw[(int64_t)gr.begin * S + t] : cw[gr.begin];
+#pragma unroll
+        for (int k = 0; k < R; ++k)
+        {
+            const float sg = ((sb >> k) & 1u) ? -1.f : 1.f;
+            wr[k][0] = sg * c.x;
+            wr[k][1] = sg * c.y;
+            wi[k][0] = sg * c.z;
+            wi[k][1] = sg * c.w;
+        }
+    }
+    for (int32_t s = gr.begin + 1; s < gr.begin + gr.count; ++s)
+    {
+        const uint32_t sb = sign_bits(recs[s], i0);
+        const float4 c = WEIGHTED ? cw[(int64_t)s * S + t] : cw[s];
+#pragma unroll
+        for (int k = 0; k < R; ++k)
+        {
+            const float sg = ((sb >> k) & 1u) ? -1.f : 1.f;
+            df_add(wr[k][0], wr[k][1], sg * c.x, sg * c.y);
+            df_add(wi[k][0], wi[k][1], sg * c.z, sg * c.w);
+        }
+    }
+}
+
+__device__ __forceinline__ float2 diag_entry(const Group &gr, const StringRec *__restrict__ recs,
+                                             const float2 *__restrict__ cw, uint64_t i)
+{
+    float wr[1], wi[1];
+    group_diag<float, 1, false>(gr, recs, cw, 1, 0, i, wr, wi);
+    return make_float2(wr[0], wi[0]);
+}
+
+__device__ __forceinline__ float4 diag_entry(const Group &gr, const StringRec *__restrict__ recs,
+                                             const float4 *__restrict__ cw, uint64_t i)
+{
+    float wr[1][2], wi[1][2];
+    group_diag_df<1, false>(gr, recs, cw, 1, 0, i, wr, wi);
+    return make_float4(wr[0][0], wr[0][1], wi[0][0], wi[0][1]);
+}
+
+// The group diagonals of a plain apply as a table diag[g * 2^n + i] =
+// (D_g)_ii (float2: complex64 sums; float4: df64 sums): they do not depend
+// on the column, so the apply kernels read them instead of summing each
+// group's strings again in every column.  Each entry is summed by the same
+// helper and in the same order as the in-register form, so both forms give
+// the same bits.  Returns at once when *skip_if is set.
+template <typename CT>
+__global__ void k_group_diag(const Group *__restrict__ groups, int64_t G, const StringRec *__restrict__ recs,
+                             const CT *__restrict__ cw, int n, CT *__restrict__ diag, const int *__restrict__ skip_if)
+{
+    if (skip_if && *skip_if)
+        return;
+    const uint64_t total = (uint64_t)G << n;
+    const uint64_t rows = (1ull << n) - 1;
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (uint64_t)gridDim.x * blockDim.x)
+        diag[e] = diag_entry(groups[e >> n], recs, cw, e & rows);
+}
+
 // only_if: when not null, the launch is the float64 form behind the df64
-// kernel and returns at once unless *only_if is set.
-template <typename T, bool WEIGHTED>
+// kernel and returns at once unless *only_if is set.  TABLE: the group
+// diagonals come from k_group_diag's table (plain apply only).
+template <typename T, bool WEIGHTED, bool TABLE = false>
 __global__ void __launch_bounds__(256)
     k_apply(const T *__restrict__ psi, T *__restrict__ out, int64_t S, int n, const Group *__restrict__ groups,
             int64_t G, const StringRec *__restrict__ recs, const typename C2<T>::type *__restrict__ cw, int TC,
-            const int *__restrict__ only_if)
+            const int *__restrict__ only_if, const typename C2<T>::type *__restrict__ diag = nullptr)
 {
+    static_assert(!(TABLE && WEIGHTED), "the diagonal table holds column-independent diagonals");
     if (only_if && *only_if == 0)
         return;
     using CT = typename C2<T>::type;
@@ -137,28 +241,22 @@ __global__ void __launch_bounds__(256)
             if (i0 + k < D)
                 b[k] = __ldg(ps + (int64_t)((i0 + k) ^ gr.x) * S + t);
         T wr[kApplyRows], wi[kApplyRows];
-#pragma unroll
-        for (int k = 0; k < kApplyRows; ++k)
-            wr[k] = wi[k] = T(0);
-        for (int32_t s = gr.begin; s < gr.begin + gr.count; ++s)
+        if constexpr (TABLE)
         {
-            const uint32_t sb = sign_bits(recs[s], i0);
-            const CT c = WEIGHTED ? cw[(int64_t)s * S + t] : cw[s];
+            const CT *dg = diag + (int64_t)g * (int64_t)D + (int64_t)i0;
 #pragma unroll
             for (int k = 0; k < kApplyRows; ++k)
             {
-                if ((sb >> k) & 1u)
-                {
-                    wr[k] -= c.x;
-                    wi[k] -= c.y;
-                }
-                else
-                {
-                    wr[k] += c.x;
-                    wi[k] += c.y;
-                }
+                CT w;
+                w.x = w.y = T(0);
+                if (i0 + k < D)
+                    w = __ldg(dg + k);
+                wr[k] = w.x;
+                wi[k] = w.y;
             }
         }
+        else
+            group_diag<T, kApplyRows, WEIGHTED>(gr, recs, cw, S, t, i0, wr, wi);
 #pragma unroll
         for (int k = 0; k < kApplyRows; ++k)
             if (i0 + k < D)
@@ -188,12 +286,15 @@ constexpr int kApplyRowsDf = 4; // output rows per thread, df64 form
 // renormalised every 16 groups, and out += sum in float64 at the end.  Error
 // ~2^-46 of sum |terms|.  Returns at once when *skip_if is set (an amplitude
 // or coefficient outside the df64 range): k_apply<double> runs instead.
-template <bool WEIGHTED>
+// TABLE: the group diagonals come from k_group_diag's table (plain apply).
+template <bool WEIGHTED, bool TABLE = false>
 __global__ void __launch_bounds__(256)
     k_apply_df(const float4 *__restrict__ psi, double *__restrict__ out, int64_t S, int n,
                const Group *__restrict__ groups, int64_t G, const StringRec *__restrict__ recs,
-               const float4 *__restrict__ cw, int TC, const int *__restrict__ skip_if)
+               const float4 *__restrict__ cw, int TC, const int *__restrict__ skip_if,
+               const float4 *__restrict__ diag = nullptr)
 {
+    static_assert(!(TABLE && WEIGHTED), "the diagonal table holds column-independent diagonals");
     if (*skip_if)
         return;
     constexpr int R = kApplyRowsDf;
@@ -220,31 +321,21 @@ __global__ void __launch_bounds__(256)
             b[k] = i0 + k < D ? __ldg(psi + (int64_t)((i0 + k) ^ gr.x) * S + t) : make_float4(0.f, 0.f, 0.f, 0.f);
         // diagonal of the group per row: sum of +-c over its strings (df64)
         float wr[R][2], wi[R][2];
+        if constexpr (TABLE)
         {
-            const uint32_t sb = sign_bits(recs[gr.begin], i0);
-            const float4 c = WEIGHTED ? cw[(int64_t)gr.begin * S + t] : cw[gr.begin];
+            const float4 *dg = diag + (int64_t)g * (int64_t)D + (int64_t)i0;
 #pragma unroll
             for (int k = 0; k < R; ++k)
             {
-                const float sg = ((sb >> k) & 1u) ? -1.f : 1.f;
-                wr[k][0] = sg * c.x;
-                wr[k][1] = sg * c.y;
-                wi[k][0] = sg * c.z;
-                wi[k][1] = sg * c.w;
+                const float4 w = i0 + k < D ? __ldg(dg + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+                wr[k][0] = w.x;
+                wr[k][1] = w.y;
+                wi[k][0] = w.z;
+                wi[k][1] = w.w;
             }
         }
-        for (int32_t s = gr.begin + 1; s < gr.begin + gr.count; ++s)
-        {
-            const uint32_t sb = sign_bits(recs[s], i0);
-            const float4 c = WEIGHTED ? cw[(int64_t)s * S + t] : cw[s];
-#pragma unroll
-            for (int k = 0; k < R; ++k)
-            {
-                const float sg = ((sb >> k) & 1u) ? -1.f : 1.f;
-                df_add(wr[k][0], wr[k][1], sg * c.x, sg * c.y);
-                df_add(wi[k][0], wi[k][1], sg * c.z, sg * c.w);
-            }
-        }
+        else
+            group_diag_df<R, WEIGHTED>(gr, recs, cw, S, t, i0, wr, wi);
         // sum += w * b  (complex, df64)
 #pragma unroll
         for (int k = 0; k < R; ++k)
@@ -376,11 +467,31 @@ int apply_lanes(int64_t S, int n, int esz)
     return tc;
 }
 
+cudaError_t launch_group_diag(bool df, const DevOp &op, const void *cw, void *diag, const int *skip_if,
+                              cudaStream_t st)
+{
+    if (op.G <= 0)
+        return cudaSuccess;
+    const uint64_t total = (uint64_t)op.G << op.n;
+    uint64_t blocks = (total + 255) / 256;
+    if (blocks > (uint64_t)sm_count() * 16)
+        blocks = (uint64_t)sm_count() * 16;
+    if (df)
+        k_group_diag<float4><<<(unsigned)blocks, 256, 0, st>>>(op.groups, op.G, op.recs, (const float4 *)cw, op.n,
+                                                               (float4 *)diag, skip_if);
+    else
+        k_group_diag<float2><<<(unsigned)blocks, 256, 0, st>>>(op.groups, op.G, op.recs, (const float2 *)cw, op.n,
+                                                               (float2 *)diag, skip_if);
+    return launched();
+}
+
 cudaError_t launch_apply(bool fp32, bool weighted, const DevOp &op, const void *cw, const void *psi, void *out,
-                         int64_t S, cudaStream_t st, const int *only_if)
+                         int64_t S, cudaStream_t st, const int *only_if, const void *diag)
 {
     if (S <= 0 || op.G <= 0)
         return cudaSuccess;
+    if (diag && (!fp32 || weighted))
+        return cudaErrorInvalidValue;
     const int TC = apply_lanes(S, op.n, fp32 ? 8 : 16);
     const int TR = 256 / TC;
     const uint64_t D = 1ull << op.n;
@@ -388,7 +499,11 @@ cudaError_t launch_apply(bool fp32, bool weighted, const DevOp &op, const void *
     dim3 grid((unsigned)((D + rows_per_cta - 1) / rows_per_cta), (unsigned)((S + TC - 1) / TC));
     if (fp32)
     {
-        if (weighted)
+        if (diag)
+            k_apply<float, false, true><<<grid, 256, 0, st>>>((const float *)psi, (float *)out, S, op.n, op.groups,
+                                                              op.G, op.recs, (const float2 *)cw, TC, only_if,
+                                                              (const float2 *)diag);
+        else if (weighted)
             k_apply<float, true><<<grid, 256, 0, st>>>((const float *)psi, (float *)out, S, op.n, op.groups, op.G,
                                                        op.recs, (const float2 *)cw, TC, only_if);
         else
@@ -408,16 +523,22 @@ cudaError_t launch_apply(bool fp32, bool weighted, const DevOp &op, const void *
 }
 
 cudaError_t launch_apply_df(bool weighted, const DevOp &op, const void *cw_df, const void *psi_df, void *out,
-                            int64_t S, const int *skip_if, cudaStream_t st)
+                            int64_t S, const int *skip_if, cudaStream_t st, const void *diag)
 {
     if (S <= 0 || op.G <= 0)
         return cudaSuccess;
+    if (diag && weighted)
+        return cudaErrorInvalidValue;
     const int TC = apply_lanes(S, op.n, 16);
     const int TR = 256 / TC;
     const uint64_t D = 1ull << op.n;
     const uint64_t rows_per_cta = (uint64_t)TR * kApplyRowsDf;
     dim3 grid((unsigned)((D + rows_per_cta - 1) / rows_per_cta), (unsigned)((S + TC - 1) / TC));
-    if (weighted)
+    if (diag)
+        k_apply_df<false, true><<<grid, 256, 0, st>>>((const float4 *)psi_df, (double *)out, S, op.n, op.groups,
+                                                      op.G, op.recs, (const float4 *)cw_df, TC, skip_if,
+                                                      (const float4 *)diag);
+    else if (weighted)
         k_apply_df<true><<<grid, 256, 0, st>>>((const float4 *)psi_df, (double *)out, S, op.n, op.groups, op.G,
                                                op.recs, (const float4 *)cw_df, TC, skip_if);
     else

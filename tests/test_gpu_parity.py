@@ -434,6 +434,46 @@ def test_float64_apply_far_from_unit_scale(scale_psi, scale_h):
     o.close()
 
 
+@pytest.mark.parametrize("n", [2, 9])
+@pytest.mark.parametrize("scale", [1.0, 1e-30])
+def test_apply_group_diagonal_table_matches_register_sums(n, scale):
+    """A plain apply of 4 or more columns whose x-groups hold two or more
+    strings on average reads the group diagonals from a table built once per
+    call (one more launch); below 4 columns every thread sums its groups'
+    strings itself.  A column's arithmetic is the same either way, so the
+    first 3 columns of an 8-column apply equal a 3-column apply bit for bit,
+    in both precisions.  n=2: fewer rows than one thread's rows; scale 1e-30:
+    the float64 range check sends both calls to the float64 kernel, which
+    never reads the table."""
+    torch = pytest.importorskip("torch")
+    from fast_pauli import _abi
+
+    L = _abi.lib()
+    rng = np.random.default_rng(71 + n)
+    strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
+    P = len(strings)
+    coeffs = rng.standard_normal(P) + 1j * rng.standard_normal(P)
+    psi = oracle.unit_norm_states(rng, 1 << n, 8) * scale
+    want = oracle.op_apply(strings, coeffs, psi)
+    op = _abi.Operator(strings)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for dtype, tdt, tol in ((_abi.FPG_C128, torch.complex128, TOL_C128), (_abi.FPG_C64, torch.complex64, TOL_MIXED)):
+        dc = torch.from_numpy(coeffs).to(tdt).cuda()
+        outs, launches = [], []
+        for S in (3, 8):
+            dpsi = torch.from_numpy(np.ascontiguousarray(psi[:, :S])).to(tdt).cuda()
+            out = torch.zeros_like(dpsi)
+            before = _abi.kernel_launches()
+            _abi.check(L.fpg_apply(op.handle, dc.data_ptr(), dpsi.data_ptr(), out.data_ptr(), S, dtype, st))
+            torch.cuda.synchronize()
+            launches.append(_abi.kernel_launches() - before)
+            outs.append(out.cpu().numpy())
+        assert launches[1] == launches[0] + 1, (dtype, launches)
+        assert np.array_equal(outs[1][:, :3], outs[0]), dtype
+        assert normwise(outs[1], want) < tol, dtype
+    op.close()
+
+
 def test_float64_contraction_mixed_magnitudes():
     """The float64 contraction scales every row of H^T and of the per-string
     expectation table by a power of two and multiplies digit slices on the
