@@ -298,6 +298,25 @@ inline cudaStream_t copy_stream()
     return h.s;
 }
 
+// A second compute stream per host thread, for work that may run beside the
+// call's stream (column chunks of one call).
+inline cudaStream_t second_stream()
+{
+    struct Holder
+    {
+        cudaStream_t s = nullptr;
+        ~Holder()
+        {
+            if (s)
+                cudaStreamDestroy(s);
+        }
+    };
+    static thread_local Holder h;
+    if (!h.s)
+        cuda_check(cudaStreamCreateWithFlags(&h.s, cudaStreamNonBlocking), "cudaStreamCreateWithFlags");
+    return h.s;
+}
+
 struct Event
 {
     cudaEvent_t e = nullptr;
@@ -1329,13 +1348,16 @@ template <std::floating_point T> struct SummedPauliOp
 
     // Host states in nc column chunks: chunk c's copy goes on the thread's
     // copy stream (the link runs the copies back to back) and its computation
-    // on the call's stream, ordered after that copy, before chunk c + 1's
+    // on a compute stream, ordered after that copy, before chunk c + 1's
     // copy is issued: from pinned memory the copies are asynchronous, and
     // from pageable memory, whose copies return only once the host has handed
     // the data over, chunk c is already running on the GPU while chunk
     // c + 1 is being copied.  The results are copied out after the last
     // chunk.  Each chunk is an independent fpg_summed_expect call on its own
-    // columns.
+    // columns; the chunks alternate between the call's stream and a second
+    // compute stream, so that a chunk whose copy has landed starts while the
+    // chunk before it runs its last, small kernels (reductions, the
+    // contraction, whose GEMM fills few SMs at a chunk's width).
     template <typename C>
     void run_expect_overlapped(fpg_operator *op, C *out, const C *psi, size_t S, bool out_zero, size_t nc,
                                cudaStream_t st) const
@@ -1373,25 +1395,32 @@ template <std::floating_point T> struct SummedPauliOp
             dout.emplace_back(K * cw[c] * el, st);
         }
         cudaStream_t cs = detail::copy_stream();
-        detail::Event fork;
+        const cudaStream_t ss[2] = {st, detail::second_stream()};
+        detail::Event fork, second_done;
         std::vector<std::unique_ptr<detail::Event>> landed(nc);
         // whatever happens below, the call's stream waits for every queued
-        // copy before the buffers go back to the pool on that stream
+        // copy and for the second compute stream before the buffers go back
+        // to the pool on the call's stream
         struct JoinCopies
         {
             std::vector<std::unique_ptr<detail::Event>> &ev;
-            cudaStream_t st;
+            cudaStream_t st, second;
+            cudaEvent_t second_done;
             ~JoinCopies()
             {
                 for (auto &e : ev)
                     if (e)
                         cudaStreamWaitEvent(st, e->e, 0);
+                if (cudaEventRecord(second_done, second) == cudaSuccess)
+                    cudaStreamWaitEvent(st, second_done, 0);
             }
-        } join{landed, st};
+        } join{landed, st, ss[1], second_done.e};
         detail::cuda_check(cudaEventRecord(fork.e, st), "cudaEventRecord");
         detail::cuda_check(cudaStreamWaitEvent(cs, fork.e, 0), "cudaStreamWaitEvent");
+        detail::cuda_check(cudaStreamWaitEvent(ss[1], fork.e, 0), "cudaStreamWaitEvent");
         for (size_t c = 0; c < nc; ++c)
         {
+            const cudaStream_t cst = ss[c & 1];
             detail::cuda_check(cudaMemcpy2DAsync(din[c].p, cw[c] * el, psi + c0[c], S * el, cw[c] * el, D,
                                                  cudaMemcpyHostToDevice, cs),
                                "cudaMemcpy2DAsync");
@@ -1405,14 +1434,16 @@ template <std::floating_point T> struct SummedPauliOp
             landed[c] = std::make_unique<detail::Event>();
             detail::cuda_check(cudaEventRecord(landed[c]->e, cs), "cudaEventRecord");
             if (out_zero)
-                detail::cuda_check(cudaMemsetAsync(dout[c].p, 0, dout[c].bytes, st), "cudaMemsetAsync");
-            detail::cuda_check(cudaStreamWaitEvent(st, landed[c]->e, 0), "cudaStreamWaitEvent");
+                detail::cuda_check(cudaMemsetAsync(dout[c].p, 0, dout[c].bytes, cst), "cudaMemsetAsync");
+            detail::cuda_check(cudaStreamWaitEvent(cst, landed[c]->e, 0), "cudaStreamWaitEvent");
             detail::check(fpg_summed_expect(op, dh.p, (int64_t)K, din[c].p, dout[c].p, (int64_t)cw[c],
-                                            detail::dtype_of<C>(), st));
+                                            detail::dtype_of<C>(), cst));
         }
         // a zero output: made resident on the host while the chunks run
         if (out_zero)
             detail::touch_host_output(out, K * S * el);
+        detail::cuda_check(cudaEventRecord(second_done.e, ss[1]), "cudaEventRecord");
+        detail::cuda_check(cudaStreamWaitEvent(st, second_done.e, 0), "cudaStreamWaitEvent");
         for (size_t c = 0; c < nc; ++c)
             detail::cuda_check(cudaMemcpy2DAsync(out + c0[c], S * el, dout[c].p, cw[c] * el, cw[c] * el, K,
                                                  cudaMemcpyDeviceToHost, st),
