@@ -607,15 +607,19 @@ ExpectPlan plan_expect(const fpg_operator *op, int64_t S, bool fp32, const void 
     // 2.048 ms at 2 / 4 / 8)
     constexpr int kSplitCtasPerSmF64Marg = 4, kSplitCtasPerSmF64Wht = 4;
     const int per_sm_all = fp32 ? kSplitCtasPerSmF32 : kSplitCtasPerSmF64;
+    // min_rounds: blocks per row lane each split keeps at least (4; the
+    // transform kernel 1: its CTAs do little per-CTA work besides the rows,
+    // and at a narrow call's few column tiles 4 rounds left most SMs idle --
+    // n=14 weight<=2, 128 states: 64 CTAs on 152 SMs, 63.5 us per launch)
     auto pick_at = [](int per_sm, int64_t ctas_per_split, int64_t blocks, int row_lanes, bool windowed,
-                      int64_t window) {
+                      int64_t window, int min_rounds = 4) {
         if (ctas_per_split <= 0)
             return 1;
         const int64_t target = (int64_t)sm_count() * per_sm;
         int64_t s = (target + ctas_per_split - 1) / ctas_per_split;
         if (windowed)
             s = std::max<int64_t>(s, (blocks + window - 1) / window);
-        const int64_t mx = std::max<int64_t>(1, blocks / ((int64_t)row_lanes * 4));
+        const int64_t mx = std::max<int64_t>(1, blocks / ((int64_t)row_lanes * min_rounds));
         return (int)std::max<int64_t>(1, std::min<int64_t>(std::min(s, mx), 65535));
     };
     auto pick = [&](int64_t ctas_per_split, int64_t blocks, int row_lanes, bool windowed, int64_t window) {
@@ -629,7 +633,7 @@ ExpectPlan plan_expect(const fpg_operator *op, int64_t S, bool fp32, const void 
                                      kWindowBlocks);
     p.fam_splits[kFamWht] = pick_at(fp32 ? kSplitCtasPerSmF32Wht : kSplitCtasPerSmF64Wht,
                                     (int64_t)op->wht.size() * p.wht_ctiles, NB16 / 2, kWhtThreads / p.wht_TC, over1,
-                                    2 * kWindowBlocks);
+                                    2 * kWindowBlocks, 1);
     // the tile kernel: one element per lane (the V = 1 tiling), its column
     // tile within the L2 budget (its units read rows spread over the whole
     // state), the df64 copy of the state for the float64 path
