@@ -30,6 +30,7 @@
 // Every mbarrier wait is bounded; on timeout the kernel records an error code
 // (fpg_device_error reports it), still waits (bounded) for its own copies and
 // MMAs, frees its TMEM and returns.
+#include <algorithm>
 #include <cstdint>
 
 #include "common.cuh"
@@ -708,19 +709,20 @@ __global__ void k_oz_slice(const void *__restrict__ src, int64_t P, int64_t widt
     }
 }
 
-// One 128 x 64 tile of one 448-deep k segment per CTA (blockIdx.z =
-// segment): the level sums accumulate in TMEM (level L at columns
-// (L-2) * 64), and the epilogue writes each output's folded double-float
-// value (hi, lo) of the segment to C[z] (rows_pad x cols_pad float2).
+// One 128 x 64 tile of one k segment (seg_chunks <= OZ_SEG_CHUNKS k chunks,
+// at most 448 deep) per CTA (blockIdx.z = segment): the level sums
+// accumulate in TMEM (level L at columns (L-2) * 64), and the epilogue writes
+// each output's folded double-float value (hi, lo) of the segment to C[z]
+// (rows_pad x cols_pad float2).
 __global__ void __launch_bounds__(128, 1)
     k_gemm_oz(const unsigned char *__restrict__ a_sl, const unsigned char *__restrict__ b_sl, int64_t kchunks,
-              int64_t mtiles, int64_t ntiles, int64_t rows_pad, int64_t cols_pad, float2 *__restrict__ C,
-              const int *__restrict__ skip_if)
+              int64_t seg_chunks, int64_t mtiles, int64_t ntiles, int64_t rows_pad, int64_t cols_pad,
+              float2 *__restrict__ C, const int *__restrict__ skip_if)
 {
     if (*skip_if)
         return;
-    const int64_t kb = (int64_t)blockIdx.z * OZ_SEG_CHUNKS;
-    const int64_t nk = min(kchunks, kb + OZ_SEG_CHUNKS) - kb; // chunks of this segment (>= 1)
+    const int64_t kb = (int64_t)blockIdx.z * seg_chunks;
+    const int64_t nk = min(kchunks, kb + seg_chunks) - kb; // chunks of this segment (>= 1)
     C += (int64_t)blockIdx.z * rows_pad * cols_pad;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -950,7 +952,7 @@ __global__ void k_oz_finish(const float2 *__restrict__ C, int64_t nseg, int64_t 
 
 struct OzLayout
 {
-    int64_t Mp, Np, Kp, kchunks, nseg;
+    int64_t Mp, Np, Kp, kchunks, seg_chunks, nseg;
     unsigned long long *max_a, *max_b;
     int *exp_a, *exp_b;
     unsigned char *a_sl, *b_sl;
@@ -964,7 +966,15 @@ OzLayout oz_layout(int64_t M, int64_t N, int64_t Kd, void *ws)
     g.Np = round_up(N, OZ_TN);
     g.Kp = round_up(Kd, OZ_TK);
     g.kchunks = g.Kp / OZ_TK;
-    g.nseg = (g.kchunks + OZ_SEG_CHUNKS - 1) / OZ_SEG_CHUNKS;
+    // segments of at most OZ_SEG_CHUNKS k chunks (their level sums stay
+    // exact); more, shorter ones while the output tiles alone would leave SMs
+    // idle (one CTA per SM: each holds all of TMEM), up to one CTA per SM --
+    // a narrow call's GEMM then takes a fraction of one long segment's time
+    const int64_t tiles = (g.Mp / OZ_TM) * (g.Np / OZ_TN);
+    int64_t nseg = (g.kchunks + OZ_SEG_CHUNKS - 1) / OZ_SEG_CHUNKS;
+    nseg = std::max<int64_t>(nseg, std::min<int64_t>(g.kchunks, (int64_t)sm_count() / std::max<int64_t>(1, tiles)));
+    g.seg_chunks = (g.kchunks + nseg - 1) / nseg;
+    g.nseg = (g.kchunks + g.seg_chunks - 1) / g.seg_chunks;
     unsigned char *p = (unsigned char *)(((uintptr_t)ws + 255) & ~(uintptr_t)255);
     g.max_a = (unsigned long long *)p;
     g.max_b = g.max_a + g.Mp;
@@ -1040,8 +1050,8 @@ cudaError_t launch_contract_oz_expect(const void *H, const double *E, int64_t P,
     if ((e = cudaFuncSetAttribute(k_gemm_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM)))
         return e;
     dim3 grid((unsigned)(g.Np / OZ_TN), (unsigned)(g.Mp / OZ_TM), (unsigned)g.nseg);
-    k_gemm_oz<<<grid, 128, OZ_SMEM, st>>>(g.a_sl, g.b_sl, g.kchunks, g.Mp / OZ_TM, g.Np / OZ_TN, g.Mp, g.Np, g.C,
-                                          flag);
+    k_gemm_oz<<<grid, 128, OZ_SMEM, st>>>(g.a_sl, g.b_sl, g.kchunks, g.seg_chunks, g.Mp / OZ_TM, g.Np / OZ_TN, g.Mp,
+                                          g.Np, g.C, flag);
     if ((e = launched()))
         return e;
     k_oz_finish<<<grid_for(K * S), 256, 0, st>>>(g.C, g.nseg, g.Mp * g.Np, g.Np, K, S, g.exp_a, g.exp_b, flag,
