@@ -439,6 +439,39 @@ def run_profile_c64(args):
     torch.cuda.synchronize()
 
 
+def run_profile_f64_calls(args):
+    """One-shot float64 cases for ncu captures on the n=14 weight<=2
+    operators (K=1000): ``apply`` = SummedPauliOp.apply of 256 states
+    (fpg_summed_apply: the group-diagonal table and the df64 apply kernel);
+    ``chunks`` = fpg_summed_expect of 128 and of 448 states, the widths of
+    the host path's column chunks.  Each: warm-up calls, then args.steps."""
+    import torch
+
+    from fast_pauli import _abi
+
+    torch.cuda.set_device(0)
+    n, K = 14, 1000
+    widths = (256,) if args.profile == "apply" else (128, 448)
+    L = _abi.lib()
+    stream = _stream_handle()
+    for S in widths:
+        strings, h, psi = weight2_problem(n=n, K=K, S=S, seed=1002)
+        op = _abi.Operator(strings)
+        dh = torch.from_numpy(h).cuda()
+        if args.profile == "apply":
+            out = torch.zeros_like(psi)
+            call = lambda: _abi.check(L.fpg_summed_apply(op.handle, dh.data_ptr(), K, psi.data_ptr(),
+                                                         out.data_ptr(), S, _abi.FPG_C128, stream))
+        else:
+            out = torch.zeros((K, S), dtype=torch.complex128, device="cuda")
+            call = lambda: _abi.check(L.fpg_summed_expect(op.handle, dh.data_ptr(), K, psi.data_ptr(),
+                                                          out.data_ptr(), S, _abi.FPG_C128, stream))
+        for _ in range(max(1, args.warmup) + args.steps):
+            call()
+        torch.cuda.synchronize()
+        op.close()
+
+
 def run_profile_batch(args):
     """One-shot case for launch lists: the 256 uneven problems as one batch
     run (default tuning) and one pass of plain per-problem calls."""
@@ -1133,11 +1166,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--profile", nargs="?", const="summed", default=None,
-                    choices=["summed", "mixed", "random", "batch"],
+                    choices=["summed", "mixed", "random", "batch", "apply", "chunks"],
                     help="short device-only run for ncu captures: summed = the n=14 weight<=2 workload (float64), "
                          "mixed = the n=18 complex64 shape (tensor-core contraction), "
                          "random = n=20, 1024 uniform random strings, 64 states, complex64, "
-                         "batch = the 256 uneven problems: one batch run and one pass of plain calls")
+                         "batch = the 256 uneven problems: one batch run and one pass of plain calls, "
+                         "apply = float64 SummedPauliOp.apply, n=14 weight<=2, 256 states, "
+                         "chunks = float64 expectation calls of 128 and 448 states (the host column chunks)")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-mixed", action="store_true")
@@ -1163,6 +1198,9 @@ def main():
         return
     if args.profile == "batch":
         run_profile_batch(args)
+        return
+    if args.profile in ("apply", "chunks"):
+        run_profile_f64_calls(args)
         return
     if args.workload != "summed" and args.impl == "ours":
         if rank == 0:
