@@ -360,7 +360,12 @@ constexpr int kApplyRowsDf = 4; // output rows per thread, df64 form
 // ~2^-46 of sum |terms|.  Returns at once when *skip_if is set (an amplitude
 // or coefficient outside the df64 range): k_apply<double> runs instead.
 // TABLE: the group diagonals come from k_group_diag's table (plain apply).
-template <bool WEIGHTED, bool TABLE = false>
+// CLASSES: the diagonals of a thread's four rows from class sums
+// (group_diag_df_classes): 2 df64 additions per string and 16 per group
+// against 8 per string, so the launch picks it for operators with 3 or more
+// strings per group on average (one kernel per choice: a per-group branch
+// between both forms measured slower than either alone).
+template <bool WEIGHTED, bool TABLE = false, bool CLASSES = false>
 __global__ void __launch_bounds__(256)
     k_apply_df(const float4 *__restrict__ psi, double *__restrict__ out, int64_t S, int n,
                const Group *__restrict__ groups, int64_t G, const StringRec *__restrict__ recs,
@@ -368,6 +373,8 @@ __global__ void __launch_bounds__(256)
                const float4 *__restrict__ diag = nullptr)
 {
     static_assert(!(TABLE && WEIGHTED), "the diagonal table holds column-independent diagonals");
+    static_assert(!(TABLE && CLASSES), "one source of diagonals");
+    static_assert(!CLASSES || kApplyRowsDf == 4, "class sums cover four rows per thread");
     if (*skip_if)
         return;
     constexpr int R = kApplyRowsDf;
@@ -407,7 +414,7 @@ __global__ void __launch_bounds__(256)
                 wi[k][1] = w.w;
             }
         }
-        else if constexpr (WEIGHTED && R == 4)
+        else if constexpr (CLASSES)
             group_diag_df_classes<WEIGHTED>(gr, recs, cw, S, t, i0, wr, wi);
         else
             group_diag_df<R, WEIGHTED>(gr, recs, cw, S, t, i0, wr, wi);
@@ -613,6 +620,10 @@ cudaError_t launch_apply_df(bool weighted, const DevOp &op, const void *cw_df, c
         k_apply_df<false, true><<<grid, 256, 0, st>>>((const float4 *)psi_df, (double *)out, S, op.n, op.groups,
                                                       op.G, op.recs, (const float4 *)cw_df, TC, skip_if,
                                                       (const float4 *)diag);
+    else if (weighted && op.P >= 3 * op.G)
+        k_apply_df<true, false, true><<<grid, 256, 0, st>>>((const float4 *)psi_df, (double *)out, S, op.n,
+                                                            op.groups, op.G, op.recs, (const float4 *)cw_df, TC,
+                                                            skip_if);
     else if (weighted)
         k_apply_df<true><<<grid, 256, 0, st>>>((const float4 *)psi_df, (double *)out, S, op.n, op.groups, op.G,
                                                op.recs, (const float4 *)cw_df, TC, skip_if);

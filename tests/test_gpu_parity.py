@@ -434,6 +434,25 @@ def test_float64_apply_far_from_unit_scale(scale_psi, scale_h):
     o.close()
 
 
+@pytest.mark.parametrize("n,S", [(2, 3), (9, 5), (9, 40), (12, 33)])
+def test_float64_apply_weighted_class_sums(n, S):
+    """A float64 apply_weighted whose operator holds 3 or more strings per
+    x-group on average sums each thread's four rows' diagonals by classes of
+    z & 3 and a 4-point transform (weight <= 2 sets); the results match the
+    oracle, also with coefficients and states far from unit scale (still
+    inside the double-float range: the weights below 2^40 with column maxima
+    above 2^-39, and the states likewise)."""
+    rng = np.random.default_rng(300 + n + S)
+    strings = oracle.calculate_pauli_strings_max_weight(n, 2)[1:]
+    P, K = len(strings), 4
+    for scale_h, scale_psi in ((1.0, 1.0), (1e8, 1e-9), (1e-9, 3.0)):
+        h = (rng.standard_normal((P, K)) + 1j * rng.standard_normal((P, K))) * scale_h
+        psi = oracle.unit_norm_states(rng, 1 << n, S) * scale_psi
+        data = rng.standard_normal((K, S))
+        got = fp.SummedPauliOp(strings, h).apply_weighted(psi, data)
+        assert normwise(got, oracle.summed_apply_weighted(strings, h, psi, data)) < TOL_C128, (scale_h, scale_psi)
+
+
 @pytest.mark.parametrize("n", [2, 9])
 @pytest.mark.parametrize("scale", [1.0, 1e-30])
 def test_apply_group_diagonal_table_matches_register_sums(n, scale):
