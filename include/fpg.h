@@ -156,6 +156,11 @@ int fpg_sparse_repr(const char *string, int32_t n_qubits, uint64_t *cols, void *
  * out(D,S) += sum_j coeffs[j] * P_j * states        (coeffs: n_strings complex)
  * Replaces PauliOp::apply (__pauli_op.hpp:399-468) and, with one string,
  * PauliString::apply_batch (__pauli_string.hpp:378-436).
+ * Scratch (this call and fpg_summed_apply): FPG_C128 takes double-float
+ * copies of the states and coefficients (16 bytes per complex element); with
+ * 4 or more states and 2 or more strings per x-group on average, a table of
+ * the x-groups' diagonals (16 bytes per group and state row for FPG_C128,
+ * 8 for FPG_C64; at most 1 GiB; left out when the pool cannot supply it).
  */
 int fpg_apply(const fpg_operator *op, const void *coeffs, const void *states, void *out, int64_t n_states,
               int32_t dtype, void *stream);
