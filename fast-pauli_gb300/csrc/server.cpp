@@ -227,8 +227,8 @@ void fpg_server::run()
         if (progressed)
             cv_done.notify_all();
         // 2. admit queued requests into free slots while the budget allows;
-        // small expectation requests admitted in this round go to one merged
-        // run on one slot
+        // small expectation requests admitted in this pass of the loop go to
+        // one merged run on one slot
         auto merge_slot = slots.end();
         std::vector<uint64_t> merge_ids;
         for (auto it = queue.begin(); it != queue.end();)
